@@ -1,0 +1,89 @@
+"""In-tree build of the CUDA engine (sm_103a) into abeille_gb300/_lib/.
+
+Three translation units are compiled in parallel with nvcc and linked into one
+shared library exposing the C-ABI of include/abeille_gb300.h:
+
+  engine.cu           host side + bookkeeping kernels     --fmad=false
+  transport_fp64.cu   FP64 parity transport kernels        --fmad=false
+  transport_mixed.cu  FP32-tracking transport kernels
+
+Host code is compiled with -ffp-contract=off so derived tables round the same
+way on x86-64 and AArch64.  A stamp of the sources and flags skips rebuilds.
+"""
+import hashlib
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+LIBDIR = os.path.join(HERE, "_lib")
+LIB = os.path.join(LIBDIR, "libabeille_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                 "-I", os.path.join(REPO, "include")]
+UNITS = [
+    ("engine.cu", ["--fmad=false"]),
+    ("transport_fp64.cu", ["--fmad=false"]),
+    ("transport_mixed.cu", []),
+]
+
+
+def nvcc():
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _stamp():
+    h = hashlib.sha256()
+    for f in sorted(os.listdir(CSRC)):
+        with open(os.path.join(CSRC, f), "rb") as fh:
+            h.update(f.encode() + fh.read())
+    with open(os.path.join(REPO, "include", "abeille_gb300.h"), "rb") as fh:
+        h.update(fh.read())
+    h.update(repr((COMMON, UNITS)).encode())
+    h.update(os.uname().machine.encode())
+    return h.hexdigest()
+
+
+def build(force=False, verbose=False):
+    os.makedirs(LIBDIR, exist_ok=True)
+    stamp_file = os.path.join(LIBDIR, "stamp")
+    stamp = _stamp()
+    if not force and os.path.exists(LIB) and os.path.exists(stamp_file):
+        with open(stamp_file) as f:
+            if f.read().strip() == stamp:
+                return LIB
+    cc = nvcc()
+    objs, procs = [], []
+    for src, extra in UNITS:
+        obj = os.path.join(LIBDIR, src.replace(".cu", ".o"))
+        cmd = [cc] + COMMON + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+        objs.append(obj)
+    failed = []
+    for src, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            failed.append((src, out.decode(errors="replace")))
+        elif verbose and out:
+            print(out.decode(errors="replace"))
+    if failed:
+        raise RuntimeError("nvcc failed:\n" + "\n".join(f"--- {s}\n{o}" for s, o in failed))
+    tmp = LIB + ".tmp"
+    subprocess.check_call([cc] + ARCH + ["-shared", "-o", tmp] + objs)
+    os.replace(tmp, LIB)
+    with open(stamp_file, "w") as f:
+        f.write(stamp)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,1548 @@
+// Host side of the GB300 multigroup transport engine: the C-ABI declared in
+// include/abeille_gb300.h, table derivation, device pools, and the
+// device-resident generation loop (bank sort, weight normalisation, entropy,
+// k and tally statistics) that replaces the reference's PowerIterator /
+// FixedSource bookkeeping.  Compiled with --fmad=false and host
+// -ffp-contract=off: every double derived here rounds as the reference's does.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "launch.h"
+
+using namespace abx;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_err;
+static int fail(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+#define CUDA_TRY(x)                                                                    \
+  do {                                                                                 \
+    cudaError_t e_ = (x);                                                              \
+    if (e_ != cudaSuccess) {                                                           \
+      return fail(e_ == cudaErrorMemoryAllocation ? ABX_ERR_OOM : ABX_ERR_CUDA,         \
+                  "%s failed: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    }                                                                                  \
+  } while (0)
+
+extern "C" const char* abx_last_error_string(void) { return g_err.c_str(); }
+extern "C" int abx_version(int* a, int* b, int* c) {
+  if (a) *a = 0;
+  if (b) *b = 4;
+  if (c) *c = 0;
+  return ABX_OK;
+}
+
+// ------------------------------------------------------- host table pools
+struct Pools {
+  std::vector<CellT> cells;
+  std::vector<int32_t> rpn;
+  std::vector<UnivT> univ;
+  std::vector<int32_t> cell_lists, lat_elems;
+  std::vector<MatT> mats;
+  std::vector<AngHdr> ang_hdr;
+  std::vector<ProbT> probs;
+  std::vector<TallyT> tallies;
+  std::vector<abx_source> sources;
+  std::vector<double> src_cdf;
+  std::vector<SurfT<double>> surf_d;
+  std::vector<LatT<double>> lat_d;
+  std::vector<double> xs_d, cdf_d, ang_d, eb_d, maj_d, dg_d, tally_eb;
+  int64_t tally_bins = 0;
+  int max_depth = 0;
+};
+
+// discrete_distribution param init (libstdc++ bits/random.tcc:2657-2678)
+static void discrete_cdf(const double* w, int n, double* cp) {
+  if (n < 2) return;
+  double sum = 0.0;
+  for (int i = 0; i < n; i++) sum += w[i];
+  double acc = 0.0;
+  for (int i = 0; i < n; i++) {
+    double p = w[i] / sum;
+    acc = (i == 0) ? p : acc + p;
+    cp[i] = acc;
+  }
+  cp[n - 1] = 1.0;
+}
+
+static double legendre_p(unsigned n, double x) {
+  // LegendreDistribution::legendre (include/materials/legendre_distribution.hpp:160-193)
+  switch (n) {
+    case 0: return 1.;
+    case 1: return x;
+    case 2: return 0.5 * (3. * x * x - 1.);
+    case 3: return 0.5 * (5. * x * x * x - 3. * x);
+    case 4: { const double x2 = x * x; return 0.125 * (35. * x2 * x2 - 30. * x2 + 3.); }
+    default: {
+      const double x2 = x * x, x3 = x2 * x, x4 = x3 * x;
+      double p3 = 0.5 * (5. * x3 - 3. * x), p4 = 0.125 * (35. * x4 - 30. * x2 + 3.);
+      unsigned l = 4;
+      while (l < n) {
+        std::swap(p3, p4);
+        p4 = ((2. * l + 1.) * x * p3 - l * p4) / (l + 1.);
+        l++;
+      }
+      return p4;
+    }
+  }
+}
+
+// LegendreDistribution::linearize (src/legendre_distribution.cpp:105-155)
+static bool linearize(const std::vector<double>& a, std::vector<double>& mu, std::vector<double>& p,
+                      std::vector<double>& c) {
+  auto pdf = [&](double m) {
+    double s = 0;
+    for (size_t l = 0; l < a.size(); l++) s += a[l] * legendre_p((unsigned)l, m);
+    return s;
+  };
+  mu = {-1., 1.};
+  p = {pdf(-1.), pdf(1.)};
+  size_t i = 0;
+  while (i < mu.size() - 1) {
+    double mid = 0.5 * (mu[i] + mu[i + 1]);
+    double pi = 0.5 * (p[i] + p[i + 1]);
+    double pr = pdf(mid);
+    double rel = std::fabs(pi - pr) / pr;
+    if (rel > 0.0001) {
+      mu.insert(mu.begin() + (long)i + 1, mid);
+      p.insert(p.begin() + (long)i + 1, pr);
+      if (mu.size() > 100000) return false;
+    } else {
+      i++;
+    }
+  }
+  c.assign(mu.size(), 0.);
+  for (size_t k = 0; k + 1 < mu.size(); k++) c[k + 1] = ((mu[k + 1] - mu[k]) * 0.5 * (p[k + 1] + p[k])) + c[k];
+  const double norm = c.back();
+  for (size_t k = 0; k < c.size(); k++) {
+    p[k] /= norm;
+    c[k] /= norm;
+  }
+  return true;
+}
+
+// Appends one problem to the pools, offsetting every index so the pools can
+// hold many problems.
+static int append_problem(Pools& P, const abx_problem* pr) {
+  if (!pr) return fail(ABX_ERR_INVALID, "null problem");
+  const abx_settings& s = pr->settings;
+  const int G = s.ngroups;
+  if (G < 1 || G > 1024) return fail(ABX_ERR_INVALID, "ngroups %d out of range", G);
+  if (s.mode != ABX_MODE_K_EIGENVALUE && s.mode != ABX_MODE_FIXED_SOURCE)
+    return fail(ABX_ERR_UNSUPPORTED, "simulation mode %d is outside the multigroup transport path", s.mode);
+  if (s.tracking != ABX_TRACK_DELTA && s.tracking != ABX_TRACK_SURFACE)
+    return fail(ABX_ERR_UNSUPPORTED, "tracking mode %d not supported", s.tracking);
+  if (!pr->energy_bounds) return fail(ABX_ERR_INVALID, "no energy bounds");
+  for (int g = 0; g < G; g++)
+    if (!(pr->energy_bounds[g] < pr->energy_bounds[g + 1]))
+      return fail(ABX_ERR_INVALID, "energy bounds must be strictly ascending");
+  if (pr->n_surfaces < 0 || pr->n_cells <= 0 || pr->n_universes <= 0 || pr->n_materials <= 0)
+    return fail(ABX_ERR_INVALID, "problem needs surfaces, cells, universes and materials");
+  if (pr->root_universe < 0 || pr->root_universe >= pr->n_universes)
+    return fail(ABX_ERR_INVALID, "root universe index %d out of range", pr->root_universe);
+  if (!(s.nparticles > 0)) return fail(ABX_ERR_INVALID, "nparticles must be positive");
+
+  const int surf0 = (int)P.surf_d.size(), cell0 = (int)P.cells.size(), univ0 = (int)P.univ.size();
+  const int mat0 = (int)P.mats.size(), lat0 = (int)P.lat_d.size();
+  // surfaces
+  for (int i = 0; i < pr->n_surfaces; i++) {
+    const abx_surface& a = pr->surfaces[i];
+    if (a.type < ABX_SURF_XPLANE || a.type > ABX_SURF_SPHERE) return fail(ABX_ERR_INVALID, "surface %d: bad type", i);
+    if (a.bc < ABX_BC_VACUUM || a.bc > ABX_BC_NORMAL) return fail(ABX_ERR_INVALID, "surface %d: bad boundary", i);
+    SurfT<double> t;
+    t.type = a.type;
+    t.bc = a.bc;
+    for (int k = 0; k < 4; k++) t.c[k] = a.c[k];
+    P.surf_d.push_back(t);
+  }
+  // cells (Cell ctor: simplify + check_for_bc, src/cell.cpp:37-67,208-246)
+  for (int i = 0; i < pr->n_cells; i++) {
+    const abx_cell& c = pr->cells[i];
+    if (c.rpn_offset < 0 || c.rpn_len < 0 || c.rpn_offset + c.rpn_len > pr->n_rpn)
+      return fail(ABX_ERR_INVALID, "cell %u: region out of range", c.id);
+    const int32_t* r = pr->rpn + c.rpn_offset;
+    bool simple = true;
+    for (int k = 0; k < c.rpn_len; k++)
+      if (r[k] == ABX_OP_COMP || r[k] == ABX_OP_UNIN) simple = false;
+    CellT t{};
+    t.rpn_off = (int)P.rpn.size();
+    int depth = 0, maxd = 0;
+    for (int k = 0; k < c.rpn_len; k++) {
+      int32_t tok = r[k];
+      if (tok >= ABX_OP_UNIN) {
+        if (tok == ABX_OP_LPAR || tok == ABX_OP_RPAR) return fail(ABX_ERR_INVALID, "cell %u: parentheses in RPN", c.id);
+        if (tok != ABX_OP_COMP) depth--;
+        if (simple) continue;
+        P.rpn.push_back(tok);
+        continue;
+      }
+      int a = tok < 0 ? -tok : tok;
+      if (a < 1 || a > pr->n_surfaces) return fail(ABX_ERR_INVALID, "cell %u: surface token %d out of range", c.id, tok);
+      int bc = pr->surfaces[a - 1].bc;
+      if (bc == ABX_BC_VACUUM || bc == ABX_BC_REFLECTIVE) t.has_bc = 1;
+      P.rpn.push_back(tok > 0 ? tok + surf0 : tok - surf0);
+      depth++;
+      maxd = std::max(maxd, depth);
+    }
+    if (!simple && maxd > 60) return fail(ABX_ERR_INVALID, "cell %u: region too deep", c.id);
+    t.rpn_len = (int)P.rpn.size() - t.rpn_off;
+    t.simple = simple;
+    t.fill_kind = c.fill_kind;
+    if (c.fill_kind == ABX_FILL_MATERIAL) {
+      if (c.fill < 0 || c.fill >= pr->n_materials) return fail(ABX_ERR_INVALID, "cell %u: material out of range", c.id);
+      t.fill = c.fill + mat0;
+    } else if (c.fill_kind == ABX_FILL_UNIVERSE) {
+      if (c.fill < 0 || c.fill >= pr->n_universes) return fail(ABX_ERR_INVALID, "cell %u: universe out of range", c.id);
+      t.fill = c.fill + univ0;
+    } else {
+      return fail(ABX_ERR_INVALID, "cell %u: bad fill kind", c.id);
+    }
+    // universe_id_to_indx[cell id] (tracker.hpp:284-285 on a Cell pad)
+    t.reentry = univ0;
+    for (int u = 0; u < pr->n_universes; u++)
+      if (pr->universes[u].id == c.id) { t.reentry = univ0 + u; break; }
+    P.cells.push_back(t);
+  }
+  // universes
+  for (int i = 0; i < pr->n_universes; i++) {
+    const abx_universe& u = pr->universes[i];
+    UnivT t{};
+    t.kind = u.kind;
+    t.outer = -1;
+    t.lat = -1;
+    if (u.kind == ABX_UNIV_CELLS) {
+      if (u.list_offset < 0 || u.list_len <= 0 || u.list_offset + u.list_len > pr->n_cell_lists)
+        return fail(ABX_ERR_INVALID, "universe %u: cell list out of range", u.id);
+      t.list_off = (int)P.cell_lists.size();
+      t.list_len = u.list_len;
+      for (int k = 0; k < u.list_len; k++) {
+        int ci = pr->cell_lists[u.list_offset + k];
+        if (ci < 0 || ci >= pr->n_cells) return fail(ABX_ERR_INVALID, "universe %u: cell index out of range", u.id);
+        P.cell_lists.push_back(ci + cell0);
+        if (P.cells[ci + cell0].has_bc) t.has_bc = 1;
+      }
+    } else if (u.kind == ABX_UNIV_RECT_LATTICE) {
+      int64_t n = (int64_t)u.shape[0] * u.shape[1] * u.shape[2];
+      if (u.shape[0] <= 0 || u.shape[1] <= 0 || u.shape[2] <= 0 || n != u.list_len ||
+          u.list_offset < 0 || u.list_offset + n > pr->n_lattice_elems)
+        return fail(ABX_ERR_INVALID, "lattice %u: shape/elements mismatch", u.id);
+      if (u.shape[0] > 1000000 || u.shape[1] > 1000000 || u.shape[2] > 1000000)
+        return fail(ABX_ERR_INVALID, "lattice %u: too many tiles along an axis", u.id);
+      t.list_off = (int)P.lat_elems.size();
+      t.list_len = (int)n;
+      for (int a = 0; a < 3; a++) t.n[a] = u.shape[a];
+      for (int64_t k = 0; k < n; k++) {
+        int e = pr->lattice_elems[u.list_offset + k];
+        if (e >= pr->n_universes) return fail(ABX_ERR_INVALID, "lattice %u: element out of range", u.id);
+        P.lat_elems.push_back(e < 0 ? -1 : e + univ0);
+      }
+      if (u.outer >= pr->n_universes) return fail(ABX_ERR_INVALID, "lattice %u: outer universe out of range", u.id);
+      t.outer = u.outer < 0 ? -1 : u.outer + univ0;
+      // RectLattice ctor (src/rect_lattice.cpp:33-52)
+      LatT<double> L;
+      for (int a = 0; a < 3; a++) {
+        if (!(u.pitch[a] > 0)) return fail(ABX_ERR_INVALID, "lattice %u: pitch must be positive", u.id);
+        L.p[a] = u.pitch[a];
+        L.pinv[a] = 1. / u.pitch[a];
+        L.lo[a] = u.origin[a] - (double)u.shape[a] * 0.5 * u.pitch[a];
+      }
+      t.lat = (int)P.lat_d.size();
+      P.lat_d.push_back(L);
+    } else {
+      return fail(ABX_ERR_INVALID, "universe %u: bad kind", u.id);
+    }
+    P.univ.push_back(t);
+  }
+  // lattices inherit their outer universe's boundary flag (src/lattice.cpp:45-53)
+  for (int pass = 0; pass < 16; pass++)
+    for (int i = univ0; i < (int)P.univ.size(); i++)
+      if (P.univ[i].kind == ABX_UNIV_RECT_LATTICE) P.univ[i].has_bc = P.univ[i].outer >= 0 ? P.univ[P.univ[i].outer].has_bc : 0;
+  (void)lat0;
+  // materials (MGNuclide ctor + get_micro_xs, src/mg_nuclide.cpp:37-118, 394-411)
+  std::vector<double> row(G), pr_row(G);
+  ProbT pt{};
+  pt.eb_off = (int)P.eb_d.size();
+  for (int g = 0; g <= G; g++) P.eb_d.push_back(pr->energy_bounds[g]);
+  pt.maj_off = (int)P.maj_d.size();
+  std::vector<double> maj(G, 0.);
+  for (int m = 0; m < pr->n_materials; m++) {
+    const abx_material& mt = pr->materials[m];
+    if (mt.n_legendre < 0 || mt.n_legendre > 5 || mt.n_delayed < 0)
+      return fail(ABX_ERR_INVALID, "material %u: bad Legendre/delayed counts", mt.id);
+    int64_t need = (int64_t)5 * G + 2LL * G * G + (int64_t)mt.n_legendre * G * G + 2LL * mt.n_delayed;
+    if (mt.data_offset < 0 || mt.data_offset + need > pr->n_mg_data)
+      return fail(ABX_ERR_INVALID, "material %u: data out of range", mt.id);
+    const double* d = pr->mg_data + mt.data_offset;
+    const double *tot = d, *abs_ = d + G, *fis = d + 2 * G, *nup = d + 3 * G, *nud = d + 4 * G;
+    const double* chi = d + 5 * G;
+    const double* sct = chi + (size_t)G * G;
+    const double* legm = sct + (size_t)G * G;
+    const double* dgp = legm + (size_t)mt.n_legendre * G * G;
+    MatT M{};
+    M.G = G;
+    M.xs_off = (int)P.xs_d.size();
+    P.xs_d.resize(P.xs_d.size() + (size_t)XS_ROWS * G);
+    double* xs = P.xs_d.data() + M.xs_off;
+    for (int g = 0; g < G; g++) {
+      xs[XS_ET * G + g] = tot[g];
+      xs[XS_EF * G + g] = fis[g];
+      xs[XS_EABS * G + g] = fis[g] + (abs_[g] - fis[g]);
+      xs[XS_NU * G + g] = nup[g] + nud[g];
+      xs[XS_NUD * G + g] = nud[g];
+      xs[XS_VEF * G + g] = 1. * (nup[g] + nud[g]) * fis[g];
+      if (fis[g] != 0. && (nup[g] + nud[g]) > 0.) M.fissile = 1;
+      if (tot[g] > maj[g]) maj[g] = tot[g];
+    }
+    M.cdf_off = (int)P.cdf_d.size();
+    P.cdf_d.resize(P.cdf_d.size() + 2 * (size_t)G * G);
+    double* cdf = P.cdf_d.data() + M.cdf_off;
+    for (int g = 0; g < G; g++) {
+      double es = 0.;
+      for (int o = 0; o < G; o++) es += sct[(size_t)g * G + o];
+      xs[XS_ES * G + g] = es;
+      for (int o = 0; o < G; o++) row[o] = sct[(size_t)g * G + o] / es;
+      discrete_cdf(row.data(), G, cdf + (size_t)g * G);
+      double ci = 0.;
+      for (int o = 0; o < G; o++) ci += chi[(size_t)g * G + o];
+      for (int o = 0; o < G; o++) row[o] = chi[(size_t)g * G + o] / ci;
+      discrete_cdf(row.data(), G, cdf + (size_t)G * G + (size_t)g * G);
+    }
+    M.ndg = mt.n_delayed;
+    M.dg_off = (int)P.dg_d.size();
+    P.dg_d.resize(P.dg_d.size() + (size_t)std::max(1, mt.n_delayed));
+    discrete_cdf(dgp, mt.n_delayed, P.dg_d.data() + M.dg_off);
+    // angle tables
+    M.ang_off = (int)P.ang_hdr.size();
+    M.iso = 1;
+    for (int gi = 0; gi < G; gi++)
+      for (int go = 0; go < G; go++) {
+        std::vector<double> a = {0.5};
+        for (int l = 1; l <= mt.n_legendre; l++) {
+          double coeff = legm[((size_t)(l - 1) * G + gi) * G + go];
+          a.resize((size_t)l + 1, 0.);
+          a[(size_t)l] = coeff * (2. * (double)l + 1.) / 2.;
+        }
+        std::vector<double> mu, pp, cc;
+        if (!linearize(a, mu, pp, cc)) return fail(ABX_ERR_INVALID, "material %u: angle table did not converge", mt.id);
+        bool iso = mu.size() == 2 && pp[0] == 0.5 && pp[1] == 0.5 && cc[0] == 0. && cc[1] == 1.;
+        if (!iso) M.iso = 0;
+        AngHdr h{(int)P.ang_d.size(), (int)mu.size()};
+        P.ang_d.insert(P.ang_d.end(), mu.begin(), mu.end());
+        P.ang_d.insert(P.ang_d.end(), pp.begin(), pp.end());
+        P.ang_d.insert(P.ang_d.end(), cc.begin(), cc.end());
+        P.ang_hdr.push_back(h);
+      }
+    P.mats.push_back(M);
+  }
+  // majorant (src/majorant.cpp:132-176)
+  for (int g = 0; g < G; g++) P.maj_d.push_back(maj[g]);
+  // tallies (src/mesh_tally.cpp:62-119)
+  pt.tally_first = (int)P.tallies.size();
+  pt.tally_count = pr->n_tallies;
+  for (int i = 0; i < pr->n_tallies; i++) {
+    const abx_mesh_tally& d = pr->tallies[i];
+    if (d.estimator != ABX_EST_COLLISION && d.estimator != ABX_EST_TRACK_LENGTH)
+      return fail(ABX_ERR_UNSUPPORTED, "tally %d: estimator not supported", i);
+    if (d.quantity < ABX_Q_FLUX || d.quantity > ABX_Q_TOTAL) return fail(ABX_ERR_UNSUPPORTED, "tally %d: quantity", i);
+    if (d.shape[0] <= 0 || d.shape[1] <= 0 || d.shape[2] <= 0 || d.n_ebounds < 2 || d.ebounds_offset < 0 ||
+        d.ebounds_offset + d.n_ebounds > pr->n_tally_ebounds)
+      return fail(ABX_ERR_INVALID, "tally %d: bad shape or energy bounds", i);
+    TallyT t{};
+    t.est = d.estimator;
+    t.quantity = d.quantity;
+    for (int a = 0; a < 3; a++) {
+      t.n[a] = d.shape[a];
+      t.low[a] = d.low[a];
+      t.hi[a] = d.hi[a];
+      t.d[a] = (d.hi[a] - d.low[a]) / (double)d.shape[a];
+      t.dinv[a] = 1. / t.d[a];
+      t.lowf[a] = (float)t.low[a];
+      t.hif[a] = (float)t.hi[a];
+      t.df[a] = (float)t.d[a];
+      t.dinvf[a] = 1.f / t.df[a];
+    }
+    t.ne = d.n_ebounds - 1;
+    t.eb_off = (int)P.tally_eb.size();
+    for (int k = 0; k < d.n_ebounds; k++) P.tally_eb.push_back(pr->tally_ebounds[d.ebounds_offset + k]);
+    t.bin_off = P.tally_bins;
+    P.tally_bins += (int64_t)t.ne * t.n[0] * t.n[1] * t.n[2];
+    if (d.estimator == ABX_EST_TRACK_LENGTH) pt.has_tle = 1;
+    else pt.has_coll = 1;
+    P.tallies.push_back(t);
+  }
+  // sources (src/simulation.cpp:58-69)
+  pt.src_first = (int)P.sources.size();
+  pt.src_count = pr->n_sources;
+  pt.src_cdf_off = (int)P.src_cdf.size();
+  {
+    std::vector<double> w(std::max(1, pr->n_sources), 0.);
+    for (int i = 0; i < pr->n_sources; i++) {
+      const abx_source& so = pr->sources[i];
+      if (so.spatial != ABX_SPATIAL_POINT && so.spatial != ABX_SPATIAL_BOX)
+        return fail(ABX_ERR_UNSUPPORTED, "source %d: spatial distribution", i);
+      if (so.direction != ABX_DIR_ISOTROPIC && so.direction != ABX_DIR_MONO)
+        return fail(ABX_ERR_UNSUPPORTED, "source %d: direction distribution", i);
+      if (so.energy != ABX_ENERGY_MONO) return fail(ABX_ERR_UNSUPPORTED, "source %d: energy distribution", i);
+      if (!(so.weight > 0)) return fail(ABX_ERR_INVALID, "source %d: weight must be positive", i);
+      P.sources.push_back(so);
+      w[i] = so.weight;
+    }
+    P.src_cdf.resize(P.src_cdf.size() + w.size());
+    discrete_cdf(w.data(), pr->n_sources, P.src_cdf.data() + pt.src_cdf_off);
+  }
+  // settings
+  pt.root = pr->root_universe + univ0;
+  pt.G = G;
+  pt.mode = s.mode;
+  pt.tracking = s.tracking;
+  pt.seed = s.seed;
+  pt.stride = s.stride;
+  pt.wgt_cutoff = s.wgt_cutoff;
+  pt.wgt_survival = s.wgt_survival;
+  pt.wgt_cutoff_f = (float)s.wgt_cutoff;
+  pt.wgt_survival_f = (float)s.wgt_survival;
+  pt.nparticles = s.nparticles;
+  pt.inv_np = 1. / s.nparticles;
+  pt.min_energy = std::max(0., pr->energy_bounds[0]);  // src/parser.cpp:157-168
+  pt.ent_on = pr->entropy.enabled;
+  for (int a = 0; a < 3; a++) {
+    pt.ent_shape[a] = pr->entropy.enabled ? pr->entropy.shape[a] : 1;
+    pt.ent_low[a] = pr->entropy.low[a];
+    pt.ent_d[a] = pr->entropy.enabled ? (pr->entropy.hi[a] - pr->entropy.low[a]) / (double)pr->entropy.shape[a] : 1.;
+  }
+  if (pr->entropy.enabled && (pr->entropy.shape[0] <= 0 || pr->entropy.shape[1] <= 0 || pr->entropy.shape[2] <= 0))
+    return fail(ABX_ERR_INVALID, "entropy mesh shape must be positive");
+  P.probs.push_back(pt);
+  return ABX_OK;
+}
+
+// ------------------------------------------------------------ device pools
+struct DevPools {
+  std::vector<void*> allocs;
+  Tables T{};
+  template <class X> int up(const std::vector<X>& v, const X** out) {
+    size_t n = std::max<size_t>(v.size(), 1);
+    void* p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, n * sizeof(X)));
+    allocs.push_back(p);
+    if (!v.empty()) CUDA_TRY(cudaMemcpy(p, v.data(), v.size() * sizeof(X), cudaMemcpyHostToDevice));
+    *out = (const X*)p;
+    return ABX_OK;
+  }
+  void release() {
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+  }
+};
+
+template <class X> static std::vector<float> to_f(const std::vector<X>& v) {
+  std::vector<float> o(v.size());
+  for (size_t i = 0; i < v.size(); i++) o[i] = (float)v[i];
+  return o;
+}
+
+static int upload(const Pools& P, DevPools& D) {
+  int rc;
+#define UP(v, dst)                                  \
+  if ((rc = D.up(v, &dst)) != ABX_OK) return rc;
+  UP(P.cells, D.T.cells);
+  UP(P.rpn, D.T.rpn);
+  UP(P.univ, D.T.univ);
+  UP(P.cell_lists, D.T.cell_lists);
+  UP(P.lat_elems, D.T.lat_elems);
+  UP(P.mats, D.T.mats);
+  UP(P.ang_hdr, D.T.ang_hdr);
+  UP(P.probs, D.T.probs);
+  UP(P.tallies, D.T.tallies);
+  UP(P.sources, D.T.sources);
+  UP(P.src_cdf, D.T.src_cdf);
+  UP(P.surf_d, D.T.surf_d);
+  UP(P.lat_d, D.T.lat_d);
+  UP(P.xs_d, D.T.xs_d);
+  UP(P.cdf_d, D.T.cdf_d);
+  UP(P.ang_d, D.T.ang_d);
+  UP(P.eb_d, D.T.eb_d);
+  UP(P.maj_d, D.T.maj_d);
+  UP(P.dg_d, D.T.dg_d);
+  UP(P.tally_eb, D.T.tally_eb);
+  // FP32 mirrors for the mixed mode
+  std::vector<SurfT<float>> sf(P.surf_d.size());
+  for (size_t i = 0; i < sf.size(); i++) {
+    sf[i].type = P.surf_d[i].type;
+    sf[i].bc = P.surf_d[i].bc;
+    for (int k = 0; k < 4; k++) sf[i].c[k] = (float)P.surf_d[i].c[k];
+  }
+  UP(sf, D.T.surf_f);
+  std::vector<LatT<float>> lf(P.lat_d.size());
+  for (size_t i = 0; i < lf.size(); i++)
+    for (int a = 0; a < 3; a++) {
+      lf[i].p[a] = (float)P.lat_d[i].p[a];
+      lf[i].lo[a] = (float)P.lat_d[i].lo[a];
+      lf[i].pinv[a] = 1.f / lf[i].p[a];
+    }
+  UP(lf, D.T.lat_f);
+  std::vector<float> xf = to_f(P.xs_d);
+  UP(xf, D.T.xs_f);
+  std::vector<float> cf = to_f(P.cdf_d);
+  UP(cf, D.T.cdf_f);
+  std::vector<float> af = to_f(P.ang_d);
+  UP(af, D.T.ang_f);
+  std::vector<float> ef = to_f(P.eb_d);
+  UP(ef, D.T.eb_f);
+  // float majorant: the rounded group maxima bound the rounded cross sections
+  std::vector<float> mf = to_f(P.maj_d);
+  UP(mf, D.T.maj_f);
+  std::vector<float> df = to_f(P.dg_d);
+  UP(df, D.T.dg_f);
+  std::vector<float> tf = to_f(P.tally_eb);
+  UP(tf, D.T.tally_eb_f);
+#undef UP
+  D.T.nprob = (int)P.probs.size();
+  return ABX_OK;
+}
+
+// ---------------------------------------------------------------- context
+template <class R> struct BankBuf {
+  BankT<R> b{};
+  size_t cap = 0;
+  std::vector<void*> mem;
+  int alloc(size_t n, bool with_prob) {
+    free_();
+    cap = n;
+    R** rs[] = {&b.x, &b.y, &b.z, &b.ux, &b.uy, &b.uz, &b.E, &b.w, &b.w2};
+    for (R** p : rs) {
+      void* m;
+      CUDA_TRY(cudaMalloc(&m, std::max<size_t>(n, 1) * sizeof(R)));
+      mem.push_back(m);
+      *p = (R*)m;
+    }
+    uint64_t** us[] = {&b.rng, &b.hid, &b.fam};
+    for (uint64_t** p : us) {
+      void* m;
+      CUDA_TRY(cudaMalloc(&m, std::max<size_t>(n, 1) * sizeof(uint64_t)));
+      mem.push_back(m);
+      *p = (uint64_t*)m;
+    }
+    b.prob = nullptr;
+    if (with_prob) {
+      void* m;
+      CUDA_TRY(cudaMalloc(&m, std::max<size_t>(n, 1) * sizeof(int32_t)));
+      mem.push_back(m);
+      b.prob = (int32_t*)m;
+    }
+    return ABX_OK;
+  }
+  void free_() {
+    for (void* m : mem) cudaFree(m);
+    mem.clear();
+    cap = 0;
+  }
+};
+
+template <class R> struct SiteBuf {
+  SiteT<R> s{};
+  size_t cap = 0;
+  std::vector<void*> mem;
+  int alloc(size_t n) {
+    free_();
+    cap = n;
+    R** rs[] = {&s.x, &s.y, &s.z, &s.ux, &s.uy, &s.uz, &s.E, &s.w};
+    for (R** p : rs) {
+      void* m;
+      CUDA_TRY(cudaMalloc(&m, std::max<size_t>(n, 1) * sizeof(R)));
+      mem.push_back(m);
+      *p = (R*)m;
+    }
+    uint32_t** us[] = {&s.hist, &s.dau};
+    for (uint32_t** p : us) {
+      void* m;
+      CUDA_TRY(cudaMalloc(&m, std::max<size_t>(n, 1) * sizeof(uint32_t)));
+      mem.push_back(m);
+      *p = (uint32_t*)m;
+    }
+    return ABX_OK;
+  }
+  void free_() {
+    for (void* m : mem) cudaFree(m);
+    mem.clear();
+    cap = 0;
+  }
+};
+
+struct RunAcc {
+  double kcol_avg, kcol_var, kabs_avg, kabs_var, ktrk_avg, ktrk_var, leak_avg, leak_var, mig_avg, mig_var;
+  int active;
+  int gen;
+  unsigned long long global_hist;
+  unsigned long long total_coll, total_flights, total_hist;
+};
+
+struct abx_context {
+  int device = 0;
+  int nsm = 152;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  Pools P;
+  DevPools D;
+  ProbT prob0{};
+  bool fissile_any = false;
+  double* tally_gen = nullptr;
+  double* tally_avg = nullptr;
+  double* tally_var = nullptr;
+  int tally_g = 0;
+  DevState* st = nullptr;
+  DevState* st_host = nullptr;
+  RunAcc* run = nullptr;
+  abx_gen_record* gen_rec = nullptr;
+  int hist_cap = 0;
+  double* ent_bins = nullptr;
+  double* ent_total = nullptr;
+  size_t ent_nbins = 0;
+  BankBuf<double> bd[2];
+  BankBuf<float> bf[2];
+  SiteBuf<double> sd;
+  SiteBuf<float> sf;
+  uint32_t* hist_count = nullptr;
+  uint32_t* offsets = nullptr;
+  uint32_t* block_sums = nullptr;
+  size_t count_cap = 0;
+  void* sec = nullptr;
+  uint32_t sec_cap = 16;
+  size_t sec_threads = 0;
+  abx_particle* aos_in = nullptr;
+  abx_site* aos_out = nullptr;
+  size_t aos_in_cap = 0, aos_out_cap = 0;
+  abx_trace_rec* trace = nullptr;
+  uint32_t trace_nhist = 0;
+  size_t trace_cap = 0;
+  int block = 256;
+  int grid = 0;
+  double last_ms = 0.;
+  uint64_t max_events = 10000000ull;
+  int prec = ABX_PREC_FP64;
+};
+
+static void ctx_free(abx_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->D.release();
+  for (auto& b : c->bd) b.free_();
+  for (auto& b : c->bf) b.free_();
+  c->sd.free_();
+  c->sf.free_();
+  void* ps[] = {c->tally_gen, c->tally_avg, c->tally_var, c->st, c->run, c->gen_rec,
+                c->ent_bins, c->ent_total, c->hist_count, c->offsets, c->block_sums, c->sec,
+                c->aos_in, c->aos_out, c->trace};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  if (c->st_host) cudaFreeHost(c->st_host);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+
+// ------------------------------------------------------------- utilities
+__global__ void k_zero_d(double* p, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = 0.;
+}
+static void zero_d(double* p, size_t n, cudaStream_t s) {
+  if (!n) return;
+  size_t b = std::min<size_t>((n + 255) / 256, 152 * 32);
+  k_zero_d<<<(unsigned)b, 256, 0, s>>>(p, n);
+}
+
+// Resets the per-step counters; the next step transports `n` histories (or the
+// device-held count when n == ~0).
+__global__ void k_step_begin(DevState* st, unsigned long long n, double kcol, int converged, int use_dev) {
+  st->next_hist = 0;
+  if (!use_dev) {
+    st->n_hist = n;
+    st->kcol = kcol;
+    st->converged = converged;
+    st->err = 0;
+    st->err_hist = 0;
+  }
+  st->site_count = 0;
+  st->site_pos = 0;
+  st->site_neg = 0;
+  st->collisions = 0;
+  st->flights = 0;
+  st->lost = 0;
+  for (int i = 0; i < 6; i++) st->scores[i] = 0.;
+  st->trace_n = 0;
+}
+
+// Exclusive scan of hist_count[0..n) (n read on the device): three phases.
+constexpr int SCAN_T = 256, SCAN_V = 8, SCAN_CHUNK = SCAN_T * SCAN_V;
+__global__ void k_scan_reduce(const uint32_t* in, const DevState* st, uint32_t* bsum) {
+  __shared__ uint32_t sh[SCAN_T];
+  const unsigned long long n = st->n_hist;
+  unsigned long long base = (unsigned long long)blockIdx.x * SCAN_CHUNK;
+  uint32_t acc = 0;
+  for (int v = 0; v < SCAN_V; v++) {
+    unsigned long long i = base + (unsigned long long)v * SCAN_T + threadIdx.x;
+    if (i < n) acc += in[i];
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = SCAN_T / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) bsum[blockIdx.x] = sh[0];
+}
+__global__ void k_scan_blocks(uint32_t* bsum, int nb) {
+  __shared__ uint32_t sh[1024];
+  // serial carry over tiles of 1024
+  uint32_t carry = 0;
+  for (int t0 = 0; t0 < nb; t0 += 1024) {
+    int i = t0 + threadIdx.x;
+    uint32_t v = i < nb ? bsum[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      uint32_t a = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += a;
+      __syncthreads();
+    }
+    if (i < nb) bsum[i] = carry + sh[threadIdx.x] - v;
+    uint32_t tot = sh[1023];
+    __syncthreads();
+    carry += tot;
+  }
+}
+__global__ void k_scan_apply(const uint32_t* in, const DevState* st, const uint32_t* bsum, uint32_t* out) {
+  __shared__ uint32_t sh[SCAN_T];
+  const unsigned long long n = st->n_hist;
+  unsigned long long base = (unsigned long long)blockIdx.x * SCAN_CHUNK + (unsigned long long)threadIdx.x * SCAN_V;
+  uint32_t loc[SCAN_V];
+  uint32_t acc = 0;
+  for (int v = 0; v < SCAN_V; v++) {
+    unsigned long long i = base + v;
+    loc[v] = i < n ? in[i] : 0;
+    acc += loc[v];
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 1; o < SCAN_T; o <<= 1) {
+    uint32_t a = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += a;
+    __syncthreads();
+  }
+  uint32_t run = bsum[blockIdx.x] + sh[threadIdx.x] - acc;
+  for (int v = 0; v < SCAN_V; v++) {
+    unsigned long long i = base + v;
+    if (i < n) out[i] = run;
+    run += loc[v];
+  }
+}
+
+// Counting sort of the fission sites into BankedParticle::operator< order
+// (include/simulation/particle.hpp:59-65), fused with the construction of the
+// next generation (src/power_iterator.cpp:359-404): weight normalisation to
+// nparticles/W, history ids in bank order, per-history skip-ahead seeding,
+// and the pre-normalisation Shannon entropy (src/entropy.cpp:32-64).
+template <class R>
+__global__ void k_next_bank(SiteT<R> S, DevState* st, const uint32_t* off, BankT<R> cur, BankT<R> nxt,
+                            const ProbT* probs, RunAcc* run, uint64_t cap, double* ent_bins, double* ent_total) {
+  const unsigned long long ns = st->site_count;
+  const ProbT& P = probs[0];
+  const double W = (double)st->site_pos - (double)st->site_neg;
+  const double wpp = P.nparticles / W;
+  const unsigned long long g0 = run->global_hist;
+  for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < ns && j < cap;
+       j += (unsigned long long)gridDim.x * blockDim.x) {
+    uint32_t h = S.hist[j];
+    uint64_t d = (uint64_t)off[h] + S.dau[j];
+    if (d >= cap) continue;
+    R x = S.x[j], y = S.y[j], z = S.z[j];
+    R ws = S.w[j];
+    nxt.x[d] = x; nxt.y[d] = y; nxt.z[d] = z;
+    nxt.ux[d] = S.ux[j]; nxt.uy[d] = S.uy[j]; nxt.uz[d] = S.uz[j];
+    nxt.E[d] = S.E[j];
+    nxt.w[d] = (R)((double)ws * wpp);
+    nxt.w2[d] = R(0);
+    uint64_t hid = g0 + d;
+    nxt.hid[d] = hid;
+    nxt.rng[d] = pcg_advance(pcg_seeded(P.seed), P.stride * hid);
+    nxt.fam[d] = cur.fam[h];
+    if (P.ent_on) {
+      int nx = (int)floor(((double)x - P.ent_low[0]) / P.ent_d[0]);
+      int ny = (int)floor(((double)y - P.ent_low[1]) / P.ent_d[1]);
+      int nz = (int)floor(((double)z - P.ent_low[2]) / P.ent_d[2]);
+      if (nx >= 0 && nx < P.ent_shape[0] && ny >= 0 && ny < P.ent_shape[1] && nz >= 0 && nz < P.ent_shape[2]) {
+        atomicAdd(ent_total, (double)ws);
+        atomicAdd(ent_bins + ((size_t)P.ent_shape[1] * P.ent_shape[2] * nx + (size_t)P.ent_shape[2] * ny + nz), (double)ws);
+      }
+    }
+  }
+}
+
+// Tallies::update_avg_and_var (src/tallies.cpp:268-280)
+__device__ void upd(int gen, double x, double& avg, double& var) {
+  double dgen = (double)gen, a0 = avg, v0 = var;
+  avg = a0 + (x - a0) / dgen;
+  if (gen > 1) var = v0 + ((x - a0) * (x - a0) / dgen) - (v0 / (dgen - 1.));
+}
+
+// End of a generation: Tallies::calc_gen_values (src/tallies.cpp:159-181),
+// Entropy::calculate_entropy (src/entropy.cpp:74-93), scalar record_generation,
+// and the bank swap bookkeeping.  One block.
+__global__ void k_gen_end(DevState* st, RunAcc* run, const ProbT* probs, abx_gen_record* rec, int hist_cap,
+                          double* ent_bins, const double* ent_total, size_t nbins, uint64_t cap, int keig,
+                          int nignored) {
+  __shared__ double sh[1024];
+  const ProbT& P = probs[0];
+  double acc = 0.;
+  double tw = ent_total ? *ent_total : 0.;
+  for (size_t b = threadIdx.x; b < nbins; b += blockDim.x) {
+    double p = fabs(ent_bins[b]) / tw;
+    if (p > 1.0) {
+    } else if (p != 0.) {
+      acc -= p * log2(p);
+    }
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < (unsigned)s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  __syncthreads();
+  for (size_t b = threadIdx.x; b < nbins; b += blockDim.x) ent_bins[b] = 0.;
+  if (threadIdx.x != 0) return;
+  const double N = P.nparticles;
+  double k_col = st->scores[0] / N, k_abs = st->scores[1] / N, k_trk = st->scores[2] / N;
+  double leak = st->scores[4] / N, mig = st->scores[5] / N;
+  int g = run->gen;  // 0-based index of this generation
+  if (g < hist_cap) {
+    abx_gen_record& r = rec[g];
+    r.kcol = k_col;
+    r.entropy = P.ent_on ? sh[0] : 0.;
+    r.collisions = st->collisions;
+    r.flights = st->flights;
+    r.histories = st->n_hist;
+    r.sites = st->site_count;
+  }
+  run->total_coll += st->collisions;
+  run->total_flights += st->flights;
+  run->total_hist += st->n_hist;
+  if (st->converged) {
+    run->active++;
+    upd(run->active, k_col, run->kcol_avg, run->kcol_var);
+    upd(run->active, k_abs, run->kabs_avg, run->kabs_var);
+    upd(run->active, k_trk, run->ktrk_avg, run->ktrk_var);
+    upd(run->active, leak, run->leak_avg, run->leak_var);
+    upd(run->active, mig, run->mig_avg, run->mig_var);
+  }
+  run->gen = g + 1;
+  if (ent_total) *(double*)ent_total = 0.;
+  if (keig) {
+    unsigned long long ns = st->site_count;
+    if (ns == 0 && st->err == 0) st->err = ABX_ERR_NO_FISSION;
+    if (ns > cap && st->err == 0) st->err = ABX_ERR_CAPACITY;
+    run->global_hist += ns;
+    st->n_hist = ns > cap ? cap : ns;
+    st->kcol = k_col;
+    st->converged = (nignored == 0) || (g + 1 >= nignored) ? 1 : 0;
+  }
+}
+
+// MeshTally::record_generation + clear_generation (src/mesh_tally.cpp:121-152)
+__global__ void k_tally_record(double* gen, double* avg, double* var, size_t n, double mult, int rec,
+                               double dg) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (rec) {
+      double old_avg = avg[i];
+      double val = gen[i] * mult;
+      double a = old_avg + (val - old_avg) / dg;
+      avg[i] = a;
+      double v = var[i];
+      v = v + (((val - old_avg) * (val - a) - (v)) / dg);
+      var[i] = v;
+    }
+    gen[i] = 0.;
+  }
+}
+
+// AoS host particles -> SoA device bank.
+template <class R> __global__ void k_bank_from_aos(const abx_particle* in, size_t n, BankT<R> b) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const abx_particle p = in[i];
+    b.x[i] = (R)p.r[0]; b.y[i] = (R)p.r[1]; b.z[i] = (R)p.r[2];
+    b.ux[i] = (R)p.u[0]; b.uy[i] = (R)p.u[1]; b.uz[i] = (R)p.u[2];
+    b.E[i] = (R)p.E; b.w[i] = (R)p.wgt; b.w2[i] = (R)p.wgt2;
+    b.rng[i] = p.rng_state; b.hid[i] = p.history_id; b.fam[i] = p.family_id;
+  }
+}
+// SoA device bank -> AoS particles.
+template <class R> __global__ void k_bank_to_aos(BankT<R> b, size_t n, abx_particle* out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    abx_particle p;
+    p.r[0] = b.x[i]; p.r[1] = b.y[i]; p.r[2] = b.z[i];
+    p.u[0] = b.ux[i]; p.u[1] = b.uy[i]; p.u[2] = b.uz[i];
+    p.E = b.E[i]; p.wgt = b.w[i]; p.wgt2 = b.w2[i];
+    p.rng_state = b.rng[i]; p.history_id = b.hid[i]; p.family_id = b.fam[i];
+    out[i] = p;
+  }
+}
+// double bank -> float bank (mixed mode source sampling)
+__global__ void k_bank_d2f(BankT<double> a, BankT<float> b, size_t off, size_t n) {
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    size_t i = off + j;
+    b.x[i] = (float)a.x[i]; b.y[i] = (float)a.y[i]; b.z[i] = (float)a.z[i];
+    b.ux[i] = (float)a.ux[i]; b.uy[i] = (float)a.uy[i]; b.uz[i] = (float)a.uz[i];
+    b.E[i] = (float)a.E[i]; b.w[i] = (float)a.w[i]; b.w2[i] = (float)a.w2[i];
+    b.rng[i] = a.rng[i]; b.hid[i] = a.hid[i]; b.fam[i] = a.fam[i];
+    if (a.prob && b.prob) b.prob[i] = a.prob[i];
+  }
+}
+// Sorted sites -> AoS BankedParticles.
+template <class R>
+__global__ void k_sites_to_aos(SiteT<R> S, const DevState* st, const uint32_t* off, BankT<R> cur, abx_site* out,
+                               uint64_t cap) {
+  const unsigned long long ns = st->site_count;
+  for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < ns;
+       j += (unsigned long long)gridDim.x * blockDim.x) {
+    uint32_t h = S.hist[j];
+    uint64_t d = (uint64_t)off[h] + S.dau[j];
+    if (d >= cap) continue;
+    abx_site s;
+    s.r[0] = S.x[j]; s.r[1] = S.y[j]; s.r[2] = S.z[j];
+    s.u[0] = S.ux[j]; s.u[1] = S.uy[j]; s.u[2] = S.uz[j];
+    s.E = S.E[j]; s.wgt = S.w[j]; s.wgt2 = 0.;
+    s.parent_history_id = cur.hid[h];
+    s.parent_daughter_id = S.dau[j];
+    s.family_id = cur.fam[h];
+    out[d] = s;
+  }
+}
+
+// ------------------------------------------------------------ ctx helpers
+
+static int ensure_counts(abx_ctx* c, size_t n) {
+  if (n <= c->count_cap) return ABX_OK;
+  size_t cap = std::max<size_t>(n, 1024);
+  if (c->hist_count) cudaFree(c->hist_count);
+  if (c->offsets) cudaFree(c->offsets);
+  if (c->block_sums) cudaFree(c->block_sums);
+  c->hist_count = c->offsets = c->block_sums = nullptr;
+  CUDA_TRY(cudaMalloc(&c->hist_count, cap * sizeof(uint32_t)));
+  CUDA_TRY(cudaMalloc(&c->offsets, cap * sizeof(uint32_t)));
+  CUDA_TRY(cudaMalloc(&c->block_sums, ((cap + SCAN_CHUNK - 1) / SCAN_CHUNK + 1) * sizeof(uint32_t)));
+  c->count_cap = cap;
+  return ABX_OK;
+}
+
+static int ensure_banks(abx_ctx* c, size_t n, bool mixed, bool with_prob) {
+  int rc;
+  for (int i = 0; i < 2; i++) {
+    if (c->bd[i].cap < n || (with_prob && !c->bd[i].b.prob))
+      if ((rc = c->bd[i].alloc(n, with_prob)) != ABX_OK) return rc;
+    if (mixed && (c->bf[i].cap < n || (with_prob && !c->bf[i].b.prob)))
+      if ((rc = c->bf[i].alloc(n, with_prob)) != ABX_OK) return rc;
+  }
+  return ensure_counts(c, n);
+}
+
+static int ensure_sites(abx_ctx* c, size_t n, bool mixed) {
+  int rc;
+  if (mixed) {
+    if (c->sf.cap < n && (rc = c->sf.alloc(n)) != ABX_OK) return rc;
+  } else {
+    if (c->sd.cap < n && (rc = c->sd.alloc(n)) != ABX_OK) return rc;
+  }
+  return ABX_OK;
+}
+
+static int ensure_sec(abx_ctx* c, bool mixed) {
+  if (c->prob0.mode != ABX_MODE_FIXED_SOURCE || !c->fissile_any) return ABX_OK;
+  size_t threads = (size_t)c->grid * c->block;
+  size_t need = threads * c->sec_cap * 9 * (mixed ? sizeof(float) : sizeof(double));
+  if (c->sec && c->sec_threads >= threads) return ABX_OK;
+  if (c->sec) cudaFree(c->sec);
+  c->sec = nullptr;
+  CUDA_TRY(cudaMalloc(&c->sec, need));
+  c->sec_threads = threads;
+  return ABX_OK;
+}
+
+static int check_state(abx_ctx* c) {
+  CUDA_TRY(cudaMemcpyAsync(c->st_host, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  int e = c->st_host->err;
+  if (e) {
+    const char* what = e == ABX_ERR_LOST_PARTICLE ? "a particle became lost"
+                       : e == ABX_ERR_MAJORANT   ? "total cross section exceeded the majorant"
+                       : e == ABX_ERR_CAPACITY   ? "fission bank or secondary stack capacity exceeded"
+                       : e == ABX_ERR_TIMEOUT    ? "a history exceeded the event limit"
+                       : e == ABX_ERR_NO_FISSION ? "No fission neutrons were produced."
+                                                 : "invalid geometry or particle state";
+    return fail(e, "%s (history %llu)", what, (unsigned long long)c->st_host->err_hist);
+  }
+  return ABX_OK;
+}
+
+template <class R> static TransportArgs<R> make_args(abx_ctx* c, const BankT<R>& bank, const SiteT<R>& sites,
+                                                     size_t site_cap) {
+  TransportArgs<R> A{};
+  A.T = c->D.T;
+  A.T.tally_gen = c->tally_gen;
+  A.bank = bank;
+  A.sites = sites;
+  A.site_cap = site_cap;
+  A.hist_count = c->hist_count;
+  A.sec = (R*)c->sec;
+  A.sec_cap = c->sec_cap;
+  A.st = c->st;
+  A.trace = c->trace_nhist ? c->trace : nullptr;
+  A.trace_nhist = c->trace_nhist;
+  A.trace_cap = c->trace_cap;
+  A.max_events = c->max_events;
+  return A;
+}
+
+static int launch_transport(abx_ctx* c, bool mixed, int which_bank, size_t site_cap) {
+  if (mixed) {
+    TransportArgs<float> A = make_args<float>(c, c->bf[which_bank].b, c->sf.s, site_cap);
+    launch_transport_f(A, c->prob0.tracking, c->trace_nhist > 0, c->grid, c->block, c->stream);
+  } else {
+    TransportArgs<double> A = make_args<double>(c, c->bd[which_bank].b, c->sd.s, site_cap);
+    launch_transport_d(A, c->prob0.tracking, c->trace_nhist > 0, c->grid, c->block, c->stream);
+  }
+  CUDA_TRY(cudaGetLastError());
+  return ABX_OK;
+}
+
+static void launch_scan(abx_ctx* c, size_t cap) {
+  unsigned nb = (unsigned)((cap + SCAN_CHUNK - 1) / SCAN_CHUNK);
+  if (nb == 0) nb = 1;
+  k_scan_reduce<<<nb, SCAN_T, 0, c->stream>>>(c->hist_count, c->st, c->block_sums);
+  k_scan_blocks<<<1, 1024, 0, c->stream>>>(c->block_sums, (int)nb);
+  k_scan_apply<<<nb, SCAN_T, 0, c->stream>>>(c->hist_count, c->st, c->block_sums, c->offsets);
+}
+
+static unsigned grid_for(size_t n) {
+  size_t b = (n + 255) / 256;
+  if (b < 1) b = 1;
+  if (b > 152 * 16) b = 152 * 16;
+  return (unsigned)b;
+}
+
+// ------------------------------------------------------------------- C-ABI
+extern "C" int abx_create(const abx_problem* problem, int device, abx_ctx** out) {
+  if (!out) return fail(ABX_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(ABX_ERR_CUDA, "no CUDA device available");
+  if (device < 0 || device >= ndev) return fail(ABX_ERR_INVALID, "device %d out of range", device);
+  abx_ctx* c = new abx_context();
+  c->device = device;
+  int rc = append_problem(c->P, problem);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  c->prob0 = c->P.probs[0];
+  for (const MatT& m : c->P.mats) c->fissile_any |= m.fissile != 0;
+  const int prec = problem->settings.precision;
+  if (prec != ABX_PREC_FP64 && prec != ABX_PREC_MIXED) {
+    delete c;
+    return fail(ABX_ERR_INVALID, "precision %d", prec);
+  }
+  c->prec = prec;
+  auto bail = [&](int code) {
+    ctx_free(c);
+    return code;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return bail(fail(ABX_ERR_CUDA, "cudaSetDevice failed"));
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, device);
+  c->nsm = prop.multiProcessorCount;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(ABX_ERR_CUDA, "stream creation failed"));
+  cudaEventCreate(&c->ev0);
+  cudaEventCreate(&c->ev1);
+  if ((rc = upload(c->P, c->D)) != ABX_OK) return bail(rc);
+  size_t nb = (size_t)std::max<int64_t>(c->P.tally_bins, 1);
+  if (cudaMalloc(&c->tally_gen, nb * 8) || cudaMalloc(&c->tally_avg, nb * 8) || cudaMalloc(&c->tally_var, nb * 8))
+    return bail(fail(ABX_ERR_OOM, "tally allocation failed"));
+  cudaMemset(c->tally_gen, 0, nb * 8);
+  cudaMemset(c->tally_avg, 0, nb * 8);
+  cudaMemset(c->tally_var, 0, nb * 8);
+  if (cudaMalloc(&c->st, sizeof(DevState)) || cudaMallocHost(&c->st_host, sizeof(DevState)) ||
+      cudaMalloc(&c->run, sizeof(RunAcc)))
+    return bail(fail(ABX_ERR_OOM, "state allocation failed"));
+  cudaMemset(c->st, 0, sizeof(DevState));
+  cudaMemset(c->run, 0, sizeof(RunAcc));
+  c->ent_nbins = problem->entropy.enabled
+                     ? (size_t)problem->entropy.shape[0] * problem->entropy.shape[1] * problem->entropy.shape[2]
+                     : 1;
+  if (cudaMalloc(&c->ent_bins, c->ent_nbins * 8) || cudaMalloc(&c->ent_total, 8))
+    return bail(fail(ABX_ERR_OOM, "entropy allocation failed"));
+  cudaMemset(c->ent_bins, 0, c->ent_nbins * 8);
+  cudaMemset(c->ent_total, 0, 8);
+  int block = problem->settings.block_size > 0 ? problem->settings.block_size : 256;
+  block = std::max(32, std::min(256, block / 32 * 32));
+  c->block = block;
+  int occ = prec == ABX_PREC_MIXED ? occupancy_f(c->prob0.tracking, block) : occupancy_d(c->prob0.tracking, block);
+  if (occ < 1) occ = 1;
+  c->grid = c->nsm * occ;
+  if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(ABX_ERR_CUDA, "device sync failed"));
+  *out = c;
+  return ABX_OK;
+}
+
+extern "C" int abx_destroy(abx_ctx* c) {
+  ctx_free(c);
+  return ABX_OK;
+}
+
+static bool mixed_of(const abx_ctx* c) { return c->prec == ABX_PREC_MIXED; }
+
+extern "C" int abx_sample_sources(abx_ctx* c, uint64_t first, size_t n, abx_particle* out) {
+  if (!c || (!out && n)) return fail(ABX_ERR_INVALID, "bad arguments");
+  if (c->prob0.src_count <= 0) return fail(ABX_ERR_INVALID, "problem has no sources");
+  if (n == 0) return ABX_OK;
+  cudaSetDevice(c->device);
+  int rc;
+  if ((rc = ensure_banks(c, n, false, false)) != ABX_OK) return rc;
+  CUDA_TRY(cudaMemsetAsync(c->st, 0, sizeof(DevState), c->stream));
+  SourceArgs S{};
+  S.T = c->D.T;
+  S.prob = 0;
+  S.first_hid = first;
+  S.n = n;
+  BankT<double>& b = c->bd[0].b;
+  S.x = b.x; S.y = b.y; S.z = b.z; S.ux = b.ux; S.uy = b.uy; S.uz = b.uz; S.E = b.E; S.w = b.w; S.w2 = b.w2;
+  S.rng = b.rng; S.hid = b.hid; S.fam = b.fam; S.probv = nullptr; S.out_off = 0; S.st = c->st;
+  launch_sources(S, c->stream);
+  if (c->aos_in_cap < n) {
+    if (c->aos_in) cudaFree(c->aos_in);
+    c->aos_in = nullptr;
+    CUDA_TRY(cudaMalloc(&c->aos_in, n * sizeof(abx_particle)));
+    c->aos_in_cap = n;
+  }
+  k_bank_to_aos<double><<<grid_for(n), 256, 0, c->stream>>>(b, n, c->aos_in);
+  CUDA_TRY(cudaGetLastError());
+  if ((rc = check_state(c)) != ABX_OK) return rc;
+  CUDA_TRY(cudaMemcpyAsync(out, c->aos_in, n * sizeof(abx_particle), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return ABX_OK;
+}
+
+extern "C" int abx_transport(abx_ctx* c, const abx_particle* bank, size_t n, double kcol, int converged,
+                             abx_site* sites, size_t site_capacity, size_t* n_sites, abx_scores* scores) {
+  if (!c || (!bank && n)) return fail(ABX_ERR_INVALID, "bad arguments");
+  if (!(kcol > 0)) return fail(ABX_ERR_INVALID, "kcol must be positive");
+  if (n > 0xffffffffull) return fail(ABX_ERR_INVALID, "at most 2^32-1 histories per call");
+  cudaSetDevice(c->device);
+  const bool mixed = mixed_of(c);
+  const bool keig = c->prob0.mode == ABX_MODE_K_EIGENVALUE;
+  int rc;
+  size_t cap = std::max<size_t>(n, 1);
+  if ((rc = ensure_banks(c, cap, mixed, false)) != ABX_OK) return rc;
+  size_t scap = keig ? std::max<size_t>(site_capacity, 1) : 1;
+  if ((rc = ensure_sites(c, scap, mixed)) != ABX_OK) return rc;
+  if ((rc = ensure_sec(c, mixed)) != ABX_OK) return rc;
+  if (c->aos_in_cap < cap) {
+    if (c->aos_in) cudaFree(c->aos_in);
+    c->aos_in = nullptr;
+    CUDA_TRY(cudaMalloc(&c->aos_in, cap * sizeof(abx_particle)));
+    c->aos_in_cap = cap;
+  }
+  if (n) CUDA_TRY(cudaMemcpyAsync(c->aos_in, bank, n * sizeof(abx_particle), cudaMemcpyHostToDevice, c->stream));
+  if (mixed) k_bank_from_aos<float><<<grid_for(n), 256, 0, c->stream>>>(c->aos_in, n, c->bf[0].b);
+  else k_bank_from_aos<double><<<grid_for(n), 256, 0, c->stream>>>(c->aos_in, n, c->bd[0].b);
+  k_step_begin<<<1, 1, 0, c->stream>>>(c->st, n, kcol, converged, 0);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+  if ((rc = launch_transport(c, mixed, 0, keig ? scap : 0)) != ABX_OK) return rc;
+  CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+  if ((rc = check_state(c)) != ABX_OK) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->last_ms = ms;
+  const DevState& h = *c->st_host;
+  size_t ns = keig ? (size_t)h.site_count : 0;
+  if (n_sites) *n_sites = ns;
+  if (scores) {
+    scores->k_col = h.scores[0];
+    scores->k_abs = h.scores[1];
+    scores->k_trk = h.scores[2];
+    scores->k_tot = h.scores[3];
+    scores->leakage = h.scores[4];
+    scores->mig_area = h.scores[5];
+    scores->collisions = h.collisions;
+    scores->flights = h.flights;
+    scores->lost = h.lost;
+  }
+  if (keig && ns > site_capacity)
+    return fail(ABX_ERR_CAPACITY, "fission bank capacity %zu < %zu sites", site_capacity, ns);
+  if (keig && ns && sites) {
+    launch_scan(c, n);
+    if (c->aos_out_cap < ns) {
+      if (c->aos_out) cudaFree(c->aos_out);
+      c->aos_out = nullptr;
+      CUDA_TRY(cudaMalloc(&c->aos_out, ns * sizeof(abx_site)));
+      c->aos_out_cap = ns;
+    }
+    if (mixed) k_sites_to_aos<float><<<grid_for(ns), 256, 0, c->stream>>>(c->sf.s, c->st, c->offsets, c->bf[0].b, c->aos_out, ns);
+    else k_sites_to_aos<double><<<grid_for(ns), 256, 0, c->stream>>>(c->sd.s, c->st, c->offsets, c->bd[0].b, c->aos_out, ns);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(sites, c->aos_out, ns * sizeof(abx_site), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+  }
+  return ABX_OK;
+}
+
+extern "C" int abx_last_transport_ms(abx_ctx* c, double* ms) {
+  if (!c || !ms) return fail(ABX_ERR_INVALID, "bad arguments");
+  *ms = c->last_ms;
+  return ABX_OK;
+}
+
+static int tally_record(abx_ctx* c, double mult, bool force) {
+  size_t n = (size_t)c->P.tally_bins;
+  if (!n) return ABX_OK;
+  k_tally_record<<<grid_for(n), 256, 0, c->stream>>>(c->tally_gen, c->tally_avg, c->tally_var, n, mult,
+                                                     force ? 1 : 0, (double)(c->tally_g + 1));
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->tally_g++;
+  return ABX_OK;
+}
+
+extern "C" int abx_tally_record_generation(abx_ctx* c, double mult) {
+  if (!c) return fail(ABX_ERR_INVALID, "null context");
+  cudaSetDevice(c->device);
+  return tally_record(c, mult, true);
+}
+
+extern "C" int abx_tally_clear_generation(abx_ctx* c) {
+  if (!c) return fail(ABX_ERR_INVALID, "null context");
+  cudaSetDevice(c->device);
+  zero_d(c->tally_gen, (size_t)c->P.tally_bins, c->stream);
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return ABX_OK;
+}
+
+extern "C" int abx_tally_size(abx_ctx* c, int id, size_t* n) {
+  if (!c || !n || id < 0 || id >= (int)c->P.tallies.size()) return fail(ABX_ERR_INVALID, "bad tally id");
+  const TallyT& t = c->P.tallies[id];
+  *n = (size_t)t.ne * t.n[0] * t.n[1] * t.n[2];
+  return ABX_OK;
+}
+
+extern "C" int abx_tally_read(abx_ctx* c, int id, double* gen, double* avg, double* var, int* generations) {
+  size_t n;
+  int rc = abx_tally_size(c, id, &n);
+  if (rc) return rc;
+  cudaSetDevice(c->device);
+  const TallyT& t = c->P.tallies[id];
+  if (gen) CUDA_TRY(cudaMemcpyAsync(gen, c->tally_gen + t.bin_off, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (avg) CUDA_TRY(cudaMemcpyAsync(avg, c->tally_avg + t.bin_off, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (var) CUDA_TRY(cudaMemcpyAsync(var, c->tally_var + t.bin_off, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (generations) *generations = c->tally_g;
+  return ABX_OK;
+}
+
+extern "C" int abx_entropy(abx_ctx* c, const abx_site* s, size_t n, double* H) {
+  // Entropy::add_point + calculate_entropy (src/entropy.cpp:32-93), Sign::Total, FP64.
+  if (!c || !H || (!s && n)) return fail(ABX_ERR_INVALID, "bad arguments");
+  const ProbT& P = c->prob0;
+  if (!P.ent_on) {
+    *H = 0.;
+    return ABX_OK;
+  }
+  size_t nb = (size_t)P.ent_shape[0] * P.ent_shape[1] * P.ent_shape[2];
+  std::vector<double> bins(nb, 0.);
+  double tw = 0.;
+  for (size_t i = 0; i < n; i++) {
+    int nx = (int)std::floor((s[i].r[0] - P.ent_low[0]) / P.ent_d[0]);
+    int ny = (int)std::floor((s[i].r[1] - P.ent_low[1]) / P.ent_d[1]);
+    int nz = (int)std::floor((s[i].r[2] - P.ent_low[2]) / P.ent_d[2]);
+    if (nx >= 0 && nx < P.ent_shape[0] && ny >= 0 && ny < P.ent_shape[1] && nz >= 0 && nz < P.ent_shape[2]) {
+      tw += s[i].wgt;
+      bins[(size_t)P.ent_shape[1] * P.ent_shape[2] * nx + (size_t)P.ent_shape[2] * ny + nz] += s[i].wgt;
+    }
+  }
+  double sum = 0.;
+  for (double b : bins) {
+    double p = std::fabs(b) / tw;
+    if (p > 1.0) {
+    } else if (p != 0.) {
+      sum -= p * std::log2(p);
+    }
+  }
+  *H = sum;
+  return ABX_OK;
+}
+
+extern "C" int abx_set_trace(abx_ctx* c, uint32_t n_hist, size_t cap) {
+  if (!c) return fail(ABX_ERR_INVALID, "null context");
+  cudaSetDevice(c->device);
+  if (c->trace) cudaFree(c->trace);
+  c->trace = nullptr;
+  c->trace_nhist = 0;
+  c->trace_cap = 0;
+  if (n_hist == 0 || cap == 0) return ABX_OK;
+  CUDA_TRY(cudaMalloc(&c->trace, cap * sizeof(abx_trace_rec)));
+  c->trace_nhist = n_hist;
+  c->trace_cap = cap;
+  return ABX_OK;
+}
+
+extern "C" int abx_get_trace(abx_ctx* c, abx_trace_rec* out, size_t cap, size_t* n_out) {
+  if (!c || !n_out) return fail(ABX_ERR_INVALID, "bad arguments");
+  cudaSetDevice(c->device);
+  CUDA_TRY(cudaMemcpy(c->st_host, c->st, sizeof(DevState), cudaMemcpyDeviceToHost));
+  size_t n = std::min<size_t>(c->st_host->trace_n, c->trace_cap);
+  *n_out = n;
+  if (!out || !c->trace) return ABX_OK;
+  std::vector<abx_trace_rec> v(n);
+  if (n) CUDA_TRY(cudaMemcpy(v.data(), c->trace, n * sizeof(abx_trace_rec), cudaMemcpyDeviceToHost));
+  // records of one history were appended in program order: a stable sort on
+  // the history index gives each history's event sequence
+  std::stable_sort(v.begin(), v.end(), [](const abx_trace_rec& a, const abx_trace_rec& b) { return a.hist < b.hist; });
+  size_t m = std::min(n, cap);
+  if (m) memcpy(out, v.data(), m * sizeof(abx_trace_rec));
+  return ABX_OK;
+}
+
+// PowerIterator::initialize + run (src/power_iterator.cpp:46-166, 305-473),
+// device resident: the host only launches.
+static int ensure_records(abx_ctx* c, int n) {
+  if (c->hist_cap >= n) return ABX_OK;
+  if (c->gen_rec) cudaFree(c->gen_rec);
+  c->gen_rec = nullptr;
+  CUDA_TRY(cudaMalloc(&c->gen_rec, (size_t)n * sizeof(abx_gen_record)));
+  CUDA_TRY(cudaMemset(c->gen_rec, 0, (size_t)n * sizeof(abx_gen_record)));
+  c->hist_cap = n;
+  return ABX_OK;
+}
+
+extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, abx_run_stats* stats,
+                                          abx_gen_record* per_gen) {
+  if (!c || ngen <= 0 || nignored < 0) return fail(ABX_ERR_INVALID, "bad arguments");
+  if (c->prob0.mode != ABX_MODE_K_EIGENVALUE) return fail(ABX_ERR_INVALID, "problem is not k-eigenvalue");
+  cudaSetDevice(c->device);
+  const bool mixed = mixed_of(c);
+  int rc;
+  const size_t N = (size_t)c->prob0.nparticles;
+  const size_t cap = 3 * N + 4096;
+  if ((rc = ensure_banks(c, cap, mixed, false)) != ABX_OK) return rc;
+  if ((rc = ensure_sites(c, cap, mixed)) != ABX_OK) return rc;
+  if ((rc = ensure_records(c, ngen)) != ABX_OK) return rc;
+  auto t0 = std::chrono::steady_clock::now();
+  CUDA_TRY(cudaMemsetAsync(c->st, 0, sizeof(DevState), c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->run, 0, sizeof(RunAcc), c->stream));
+  zero_d(c->tally_gen, (size_t)c->P.tally_bins, c->stream);
+  zero_d(c->tally_avg, (size_t)c->P.tally_bins, c->stream);
+  zero_d(c->tally_var, (size_t)c->P.tally_bins, c->stream);
+  c->tally_g = 0;
+  // initial source bank, histories 0..N-1 (src/power_iterator.cpp:135-166)
+  SourceArgs S{};
+  S.T = c->D.T;
+  S.prob = 0;
+  S.first_hid = 0;
+  S.n = N;
+  BankT<double>& b0 = c->bd[0].b;
+  S.x = b0.x; S.y = b0.y; S.z = b0.z; S.ux = b0.ux; S.uy = b0.uy; S.uz = b0.uz; S.E = b0.E; S.w = b0.w;
+  S.w2 = b0.w2; S.rng = b0.rng; S.hid = b0.hid; S.fam = b0.fam; S.probv = nullptr; S.out_off = 0; S.st = c->st;
+  launch_sources(S, c->stream);
+  if (mixed) k_bank_d2f<<<grid_for(N), 256, 0, c->stream>>>(b0, c->bf[0].b, 0, N);
+  {
+    // RunAcc.global_hist = N; DevState: n_hist = N, kcol = 1, converged
+    RunAcc ra{};
+    ra.global_hist = N;
+    CUDA_TRY(cudaMemcpyAsync(c->run, &ra, sizeof ra, cudaMemcpyHostToDevice, c->stream));
+  }
+  if ((rc = check_state(c)) != ABX_OK) return rc;
+  k_step_begin<<<1, 1, 0, c->stream>>>(c->st, N, 1.0, nignored == 0 ? 1 : 0, 0);
+  if ((rc = ensure_sec(c, mixed)) != ABX_OK) return rc;
+  std::vector<cudaEvent_t> evs(4 * (size_t)ngen);
+  for (auto& e : evs) cudaEventCreate(&e);
+  int cur = 0;
+  int active_tally = 0;
+  for (int g = 1; g <= ngen; g++) {
+    cudaEventRecord(evs[4 * (g - 1)], c->stream);
+    k_step_begin<<<1, 1, 0, c->stream>>>(c->st, 0, 0., 0, 1);
+    cudaEventRecord(evs[4 * (g - 1) + 1], c->stream);
+    if ((rc = launch_transport(c, mixed, cur, cap)) != ABX_OK) break;
+    cudaEventRecord(evs[4 * (g - 1) + 2], c->stream);
+    launch_scan(c, cap);
+    if (mixed)
+      k_next_bank<float><<<grid_for(cap), 256, 0, c->stream>>>(c->sf.s, c->st, c->offsets, c->bf[cur].b,
+                                                               c->bf[1 - cur].b, c->D.T.probs, c->run, cap,
+                                                               c->ent_bins, c->ent_total);
+    else
+      k_next_bank<double><<<grid_for(cap), 256, 0, c->stream>>>(c->sd.s, c->st, c->offsets, c->bd[cur].b,
+                                                                c->bd[1 - cur].b, c->D.T.probs, c->run, cap,
+                                                                c->ent_bins, c->ent_total);
+    // tallies: record when this generation is active, always clear
+    bool conv = (nignored == 0) || (g > nignored);
+    if (c->P.tally_bins) {
+      if (conv) active_tally++;
+      k_tally_record<<<grid_for((size_t)c->P.tally_bins), 256, 0, c->stream>>>(
+          c->tally_gen, c->tally_avg, c->tally_var, (size_t)c->P.tally_bins, 1.0, conv ? 1 : 0,
+          (double)std::max(active_tally, 1));
+    }
+    k_gen_end<<<1, 1024, 0, c->stream>>>(c->st, c->run, c->D.T.probs, c->gen_rec, c->hist_cap, c->ent_bins,
+                                         c->ent_total, c->ent_nbins, cap, 1, nignored);
+    cudaEventRecord(evs[4 * (g - 1) + 3], c->stream);
+    CUDA_TRY(cudaGetLastError());
+    cur = 1 - cur;
+    if ((g & 7) == 0 || g == ngen) {
+      if ((rc = check_state(c)) != ABX_OK) break;
+    }
+  }
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->tally_g = active_tally;
+  double tms = 0.;
+  std::vector<abx_gen_record> recs(ngen);
+  if (rc == ABX_OK) CUDA_TRY(cudaMemcpy(recs.data(), c->gen_rec, ngen * sizeof(abx_gen_record), cudaMemcpyDeviceToHost));
+  for (int g = 0; g < ngen && rc == ABX_OK; g++) {
+    float ms = 0.f, ts = 0.f;
+    cudaEventElapsedTime(&ms, evs[4 * g], evs[4 * g + 3]);
+    cudaEventElapsedTime(&ts, evs[4 * g + 1], evs[4 * g + 2]);
+    recs[g].step_ms = ms;
+    recs[g].transport_ms = ts;
+    tms += ts;
+  }
+  for (auto& e : evs) cudaEventDestroy(e);
+  if (rc) return rc;
+  auto t1 = std::chrono::steady_clock::now();
+  RunAcc ra;
+  CUDA_TRY(cudaMemcpy(&ra, c->run, sizeof ra, cudaMemcpyDeviceToHost));
+  if (per_gen) memcpy(per_gen, recs.data(), ngen * sizeof(abx_gen_record));
+  if (stats) {
+    memset(stats, 0, sizeof *stats);
+    stats->generations = ra.gen;
+    stats->active = ra.active;
+    stats->kcol_avg = ra.kcol_avg;
+    stats->kcol_std = ra.active ? std::sqrt(ra.kcol_var / ra.active) : 0.;
+    stats->ktrk_avg = ra.ktrk_avg;
+    stats->ktrk_std = ra.active ? std::sqrt(ra.ktrk_var / ra.active) : 0.;
+    stats->leak_avg = ra.leak_avg;
+    stats->leak_std = ra.active ? std::sqrt(ra.leak_var / ra.active) : 0.;
+    stats->mig_avg = ra.mig_avg;
+    stats->mig_std = ra.active ? std::sqrt(ra.mig_var / ra.active) : 0.;
+    stats->collisions = ra.total_coll;
+    stats->flights = ra.total_flights;
+    stats->histories = ra.total_hist;
+    stats->transport_ms = tms;
+    stats->total_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  }
+  return ABX_OK;
+}
+
+extern "C" int abx_run_power_iteration(abx_ctx* c, int ngen, int nignored, abx_run_stats* stats, double* kcol_gen,
+                                       double* ent_gen) {
+  if (ngen <= 0) return fail(ABX_ERR_INVALID, "bad arguments");
+  std::vector<abx_gen_record> r(ngen);
+  int rc = abx_run_power_iteration_ex(c, ngen, nignored, stats, r.data());
+  if (rc) return rc;
+  for (int g = 0; g < ngen; g++) {
+    if (kcol_gen) kcol_gen[g] = r[g].kcol;
+    if (ent_gen) ent_gen[g] = r[g].entropy;
+  }
+  return ABX_OK;
+}
+
+// FixedSource::run (src/fixed_source.cpp:81-173): batches of fresh source
+// histories; fission makes in-history secondaries.
+extern "C" int abx_run_fixed_source(abx_ctx* c, int nbatches, uint64_t npart, abx_run_stats* stats) {
+  if (!c || nbatches <= 0 || npart == 0) return fail(ABX_ERR_INVALID, "bad arguments");
+  if (c->prob0.mode != ABX_MODE_FIXED_SOURCE) return fail(ABX_ERR_INVALID, "problem is not fixed-source");
+  cudaSetDevice(c->device);
+  const bool mixed = mixed_of(c);
+  int rc;
+  if ((rc = ensure_banks(c, npart, mixed, false)) != ABX_OK) return rc;
+  if ((rc = ensure_sites(c, 1, mixed)) != ABX_OK) return rc;
+  if ((rc = ensure_sec(c, mixed)) != ABX_OK) return rc;
+  if ((rc = ensure_records(c, nbatches)) != ABX_OK) return rc;
+  auto t0 = std::chrono::steady_clock::now();
+  CUDA_TRY(cudaMemsetAsync(c->st, 0, sizeof(DevState), c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->run, 0, sizeof(RunAcc), c->stream));
+  zero_d(c->tally_gen, (size_t)c->P.tally_bins, c->stream);
+  zero_d(c->tally_avg, (size_t)c->P.tally_bins, c->stream);
+  zero_d(c->tally_var, (size_t)c->P.tally_bins, c->stream);
+  c->tally_g = 0;
+  std::vector<cudaEvent_t> evs(2 * (size_t)nbatches);
+  for (auto& e : evs) cudaEventCreate(&e);
+  uint64_t hc = 0;
+  for (int g = 1; g <= nbatches; g++) {
+    SourceArgs S{};
+    S.T = c->D.T;
+    S.prob = 0;
+    S.first_hid = hc;
+    S.n = npart;
+    BankT<double>& b0 = c->bd[0].b;
+    S.x = b0.x; S.y = b0.y; S.z = b0.z; S.ux = b0.ux; S.uy = b0.uy; S.uz = b0.uz; S.E = b0.E; S.w = b0.w;
+    S.w2 = b0.w2; S.rng = b0.rng; S.hid = b0.hid; S.fam = b0.fam; S.probv = nullptr; S.out_off = 0; S.st = c->st;
+    launch_sources(S, c->stream);
+    if (mixed) k_bank_d2f<<<grid_for(npart), 256, 0, c->stream>>>(b0, c->bf[0].b, 0, npart);
+    hc += npart;
+    k_step_begin<<<1, 1, 0, c->stream>>>(c->st, npart, 1.0, 1, 0);
+    cudaEventRecord(evs[2 * (g - 1)], c->stream);
+    if ((rc = launch_transport(c, mixed, 0, 0)) != ABX_OK) break;
+    cudaEventRecord(evs[2 * (g - 1) + 1], c->stream);
+    if (c->P.tally_bins)
+      k_tally_record<<<grid_for((size_t)c->P.tally_bins), 256, 0, c->stream>>>(
+          c->tally_gen, c->tally_avg, c->tally_var, (size_t)c->P.tally_bins, 1.0, 1, (double)g);
+    k_gen_end<<<1, 1024, 0, c->stream>>>(c->st, c->run, c->D.T.probs, c->gen_rec, c->hist_cap, c->ent_bins,
+                                         nullptr, 0, npart, 0, 0);
+    CUDA_TRY(cudaGetLastError());
+    if ((rc = check_state(c)) != ABX_OK) break;
+  }
+  double tms = 0.;
+  for (int g = 0; g < nbatches && rc == ABX_OK; g++) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, evs[2 * g], evs[2 * g + 1]);
+    tms += ms;
+  }
+  for (auto& e : evs) cudaEventDestroy(e);
+  if (rc) return rc;
+  c->tally_g = nbatches;
+  auto t1 = std::chrono::steady_clock::now();
+  RunAcc ra;
+  CUDA_TRY(cudaMemcpy(&ra, c->run, sizeof ra, cudaMemcpyDeviceToHost));
+  if (stats) {
+    memset(stats, 0, sizeof *stats);
+    stats->generations = ra.gen;
+    stats->active = ra.active;
+    stats->leak_avg = ra.leak_avg;
+    stats->leak_std = ra.active ? std::sqrt(ra.leak_var / ra.active) : 0.;
+    stats->mig_avg = ra.mig_avg;
+    stats->mig_std = ra.active ? std::sqrt(ra.mig_var / ra.active) : 0.;
+    stats->collisions = ra.total_coll;
+    stats->flights = ra.total_flights;
+    stats->histories = ra.total_hist;
+    stats->transport_ms = tms;
+    stats->total_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  }
+  return ABX_OK;
+}

@@ -1,0 +1,43 @@
+// Host-side launchers exported by the kernel translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tables.h"
+
+namespace abx {
+
+template <class R> struct TransportArgs;
+template <class R> struct BankT;
+
+struct SourceArgs {
+  Tables T;
+  int prob;                 // problem index whose sources are sampled
+  uint64_t first_hid;
+  uint64_t n;
+  // output bank (double SoA)
+  double *x, *y, *z, *ux, *uy, *uz, *E, *w, *w2;
+  uint64_t* rng;
+  uint64_t* hid;
+  uint64_t* fam;
+  int32_t* probv;           // optional per-history problem index output
+  uint64_t out_off;         // write offset into the output arrays
+  DevState* st;
+};
+
+// transport_fp64.cu
+void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace, int grid, int block,
+                        cudaStream_t s);
+void launch_sources(const SourceArgs& A, cudaStream_t s);
+int transport_regs_d(int tracking);
+
+// transport_mixed.cu
+void launch_transport_f(const TransportArgs<float>& A, int tracking, bool trace, int grid, int block,
+                        cudaStream_t s);
+int transport_regs_f(int tracking);
+
+// occupancy helpers
+int occupancy_d(int tracking, int block);
+int occupancy_f(int tracking, int block);
+
+}  // namespace abx

@@ -1,0 +1,181 @@
+"""Python face of the C-ABI, shaped like the reference's plugin interface.
+
+``Engine`` owns one abx context (one problem on one GPU).  On top of it:
+
+* ``GpuDeltaTracker`` / ``GpuSurfaceTracker`` mirror ``Transporter::transport``
+  (include/simulation/transporter.hpp:78-81): they take a bank of particles and
+  return the fission bank in the reference's order;
+* ``PowerIterator`` / ``FixedSource`` mirror the drivers
+  (src/power_iterator.cpp:305-473, src/fixed_source.cpp:81-173) and run fully
+  on the device.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+PARTICLE_DTYPE = np.dtype([("r", "<f8", 3), ("u", "<f8", 3), ("E", "<f8"), ("wgt", "<f8"), ("wgt2", "<f8"),
+                           ("history_id", "<u8"), ("rng_state", "<u8"), ("family_id", "<u8")])
+SITE_DTYPE = np.dtype([("r", "<f8", 3), ("u", "<f8", 3), ("E", "<f8"), ("wgt", "<f8"), ("wgt2", "<f8"),
+                       ("parent_history_id", "<u8"), ("parent_daughter_id", "<u8"), ("family_id", "<u8")])
+TRACE_DTYPE = np.dtype([("hist", "<u4"), ("kind", "<i4"), ("group", "<i4"), ("cell", "<i4"),
+                        ("rng_state", "<u8"), ("r", "<f8", 3), ("u", "<f8", 3), ("wgt", "<f8")])
+assert PARTICLE_DTYPE.itemsize == C.sizeof(abi.Particle)
+assert SITE_DTYPE.itemsize == C.sizeof(abi.Site)
+assert TRACE_DTYPE.itemsize == C.sizeof(abi.TraceRec)
+
+
+def scores_dict(s):
+    return {f: getattr(s, f) for f, _ in abi.Scores._fields_}
+
+
+def stats_dict(s):
+    return {f: getattr(s, f) for f, _ in abi.RunStats._fields_}
+
+
+class Engine:
+    """One problem resident on one GPU."""
+
+    def __init__(self, built, device=0):
+        self.lib = abi.load()
+        self.built = built
+        self.ctx = C.c_void_p()
+        abi.check(self.lib.abx_create(built.ptr, device, C.byref(self.ctx)), self.lib)
+
+    def close(self):
+        if self.ctx:
+            self.lib.abx_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        abi.check(rc, self.lib)
+
+    def sample_sources(self, first, n):
+        out = np.zeros(n, PARTICLE_DTYPE)
+        self._chk(self.lib.abx_sample_sources(self.ctx, first, n, out.ctypes.data_as(C.POINTER(abi.Particle))))
+        return out
+
+    def transport(self, bank, kcol=1.0, converged=True, site_capacity=None):
+        bank = np.ascontiguousarray(bank, PARTICLE_DTYPE)
+        n = bank.size
+        cap = site_capacity if site_capacity is not None else 4 * n + 64
+        sites = np.zeros(max(cap, 1), SITE_DTYPE)
+        ns = C.c_size_t(0)
+        sc = abi.Scores()
+        self._chk(self.lib.abx_transport(self.ctx, bank.ctypes.data_as(C.POINTER(abi.Particle)), n, float(kcol),
+                                         int(bool(converged)), sites.ctypes.data_as(C.POINTER(abi.Site)), cap,
+                                         C.byref(ns), C.byref(sc)))
+        return sites[: ns.value].copy(), scores_dict(sc)
+
+    def last_transport_ms(self):
+        ms = C.c_double()
+        self._chk(self.lib.abx_last_transport_ms(self.ctx, C.byref(ms)))
+        return ms.value
+
+    def tally(self, tid=0):
+        n = C.c_size_t()
+        self._chk(self.lib.abx_tally_size(self.ctx, tid, C.byref(n)))
+        gen, avg, var = (np.zeros(n.value) for _ in range(3))
+        g = C.c_int()
+        self._chk(self.lib.abx_tally_read(self.ctx, tid, gen.ctypes.data, avg.ctypes.data, var.ctypes.data,
+                                          C.byref(g)))
+        return {"gen": gen, "avg": avg, "var": var, "generations": g.value}
+
+    def record_generation(self, multiplier=1.0):
+        self._chk(self.lib.abx_tally_record_generation(self.ctx, multiplier))
+
+    def clear_generation(self):
+        self._chk(self.lib.abx_tally_clear_generation(self.ctx))
+
+    def entropy(self, sites):
+        sites = np.ascontiguousarray(sites, SITE_DTYPE)
+        h = C.c_double()
+        self._chk(self.lib.abx_entropy(self.ctx, sites.ctypes.data_as(C.POINTER(abi.Site)), sites.size, C.byref(h)))
+        return h.value
+
+    def run_power_iteration(self, ngenerations, nignored):
+        st = abi.RunStats()
+        k = np.zeros(ngenerations)
+        h = np.zeros(ngenerations)
+        self._chk(self.lib.abx_run_power_iteration(self.ctx, ngenerations, nignored, C.byref(st), k.ctypes.data,
+                                                   h.ctypes.data))
+        return stats_dict(st), k, h
+
+    def run_power_iteration_records(self, ngenerations, nignored):
+        st = abi.RunStats()
+        recs = (abi.GenRecord * ngenerations)()
+        self._chk(self.lib.abx_run_power_iteration_ex(self.ctx, ngenerations, nignored, C.byref(st), recs))
+        rows = [{f: getattr(r, f) for f, _ in abi.GenRecord._fields_} for r in recs]
+        return stats_dict(st), rows
+
+    def run_fixed_source(self, nbatches, nparticles):
+        st = abi.RunStats()
+        self._chk(self.lib.abx_run_fixed_source(self.ctx, nbatches, nparticles, C.byref(st)))
+        return stats_dict(st)
+
+    def set_trace(self, n_hist, capacity=1 << 20):
+        self._chk(self.lib.abx_set_trace(self.ctx, n_hist, capacity))
+
+    def get_trace(self):
+        n = C.c_size_t()
+        self._chk(self.lib.abx_get_trace(self.ctx, None, 0, C.byref(n)))
+        out = np.zeros(n.value, TRACE_DTYPE)
+        self._chk(self.lib.abx_get_trace(self.ctx, out.ctypes.data_as(C.POINTER(abi.TraceRec)), n.value,
+                                         C.byref(n)))
+        return out
+
+
+class _GpuTracker:
+    """Transporter::transport on the GPU: consumes the bank, returns the
+    fission bank in BankedParticle::operator< order."""
+
+    tracking = None
+
+    def __init__(self, engine, tallies=None):
+        self.engine = engine
+        self.tallies = tallies if tallies is not None else {"kcol": 1.0, "converged": False}
+        self.last_scores = None
+
+    def transport(self, bank, noise=False, noise_bank=None, noise_maker=None):
+        if noise or noise_bank is not None or noise_maker is not None:
+            raise abi.AbxError(9, "noise transport is outside the multigroup transport path")
+        sites, scores = self.engine.transport(bank, self.tallies["kcol"], self.tallies["converged"])
+        self.last_scores = scores
+        return sites
+
+
+class GpuDeltaTracker(_GpuTracker):
+    tracking = "delta-tracking"
+
+
+class GpuSurfaceTracker(_GpuTracker):
+    tracking = "surface-tracking"
+
+
+class PowerIterator:
+    """PowerIterator::run on the device (bank, sort, normalisation, entropy,
+    tallies resident in HBM)."""
+
+    def __init__(self, engine, ngenerations, nignored):
+        self.engine, self.ngenerations, self.nignored = engine, ngenerations, nignored
+
+    def run(self):
+        stats, kcol, entropy = self.engine.run_power_iteration(self.ngenerations, self.nignored)
+        self.stats, self.kcol, self.entropy = stats, kcol, entropy
+        return stats
+
+
+class FixedSource:
+    def __init__(self, engine, nbatches, nparticles):
+        self.engine, self.nbatches, self.nparticles = engine, nbatches, nparticles
+
+    def run(self):
+        self.stats = self.engine.run_fixed_source(self.nbatches, self.nparticles)
+        return self.stats

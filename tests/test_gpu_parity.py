@@ -1,0 +1,166 @@
+"""Parity of the CUDA engine with the oracle, through the C-ABI.
+
+FP64 mode: integers (rng states, event kinds, groups, cells, history and
+daughter ids, collision counts) are compared bit-exactly; floating values
+within 1e-12 relative (the engine calls CUDA's log/sin/cos where the
+reference calls glibc's, which differ in the last bit on some inputs).
+Tallies and scores are compared within 1e-12 relative, which absorbs the
+order of atomic additions.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from abeille_gb300 import Engine, decks
+from abeille_gb300.abi import AbxError
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+DECKS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_decks.json")))
+
+
+def pair(builder, precision="fp64", nthreads=1):
+    built = builder.build(precision=precision)
+    return Engine(built, 0), oracle.Oracle(built, nthreads=nthreads), built
+
+
+def close(a, b, rtol=RTOL, atol=1e-10):
+    return np.allclose(a, b, rtol=rtol, atol=atol)
+
+
+def compare_traces(tg, tc):
+    assert len(tg) == len(tc), (len(tg), len(tc))
+    for f in ("hist", "kind", "group", "cell", "rng_state"):
+        assert np.array_equal(tg[f], tc[f]), f
+    assert close(tg["r"], tc["r"], atol=1e-9)
+    assert close(tg["u"], tc["u"], atol=1e-9)
+    assert close(tg["wgt"], tc["wgt"])
+
+
+@pytest.mark.parametrize("cfg", [0, 2])
+def test_source_sampling_matches(cfg):
+    b = decks.CONFIGS[cfg](nparticles=4096)
+    eng, ora, _ = pair(b)
+    g = eng.sample_sources(123, 4096)
+    c = ora.sample_sources(123, 4096)
+    assert np.array_equal(g["rng_state"], c["rng_state"])
+    assert np.array_equal(g["history_id"], c["history_id"])
+    assert close(g["r"], c["r"]) and close(g["u"], c["u"])
+    assert np.array_equal(g["E"], c["E"])
+
+
+@pytest.mark.parametrize("cfg,tracking", [(0, "delta-tracking"), (0, "surface-tracking"),
+                                          (2, "delta-tracking"), (2, "surface-tracking")])
+def test_event_traces_match_per_history(cfg, tracking):
+    b = decks.CONFIGS[cfg](nparticles=256, tracking=tracking)
+    eng, ora, _ = pair(b)
+    bank = ora.sample_sources(0, 256)
+    eng.set_trace(64, 1 << 20)
+    ora.set_trace(64, 1 << 20)
+    eng.transport(bank, 1.0, True)
+    ora.transport(bank, 1.0, True)
+    compare_traces(eng.get_trace(), ora.get_trace())
+
+
+@pytest.mark.parametrize("cfg,tracking", [(0, "delta-tracking"), (1, "delta-tracking"), (2, "surface-tracking"),
+                                          (2, "delta-tracking")])
+def test_transport_step_matches(cfg, tracking):
+    n = 4096 if cfg != 2 else 1024
+    b = decks.CONFIGS[cfg](nparticles=n, tracking=tracking)
+    eng, ora, _ = pair(b, nthreads=oracle.cores())
+    bank = ora.sample_sources(0, n)
+    sg, cg = eng.transport(bank, 1.1, True)
+    sc, cc = ora.transport(bank, 1.1, True)
+    assert len(sg) == len(sc)
+    assert np.array_equal(sg["parent_history_id"], sc["parent_history_id"])
+    assert np.array_equal(sg["parent_daughter_id"], sc["parent_daughter_id"])
+    assert np.array_equal(sg["wgt"], sc["wgt"]) and np.array_equal(sg["E"], sc["E"])
+    assert close(sg["r"], sc["r"], atol=1e-9) and close(sg["u"], sc["u"], atol=1e-9)
+    for k in ("collisions", "flights", "lost"):
+        assert cg[k] == cc[k], k
+    for k in ("k_col", "k_abs", "k_trk", "leakage", "mig_area"):
+        assert abs(cg[k] - cc[k]) <= RTOL * abs(cc[k]) + 1e-300, (k, cg[k], cc[k])
+    assert close(eng.tally(0)["gen"], ora.tally(0)["gen"], atol=0.0)
+
+
+def test_power_iteration_matches():
+    b = decks.config0(nparticles=2000)
+    eng, ora, _ = pair(b, nthreads=oracle.cores())
+    sg, kg, hg = eng.run_power_iteration(6, 2)
+    sc, kc, hc = ora.run_power_iteration(6, 2)
+    assert np.allclose(kg, kc, rtol=1e-11, atol=0)
+    assert np.allclose(hg, hc, rtol=1e-11, atol=0)
+    assert sg["collisions"] == sc["collisions"] and sg["histories"] == sc["histories"]
+    assert abs(sg["kcol_avg"] - sc["kcol_avg"]) <= 1e-11 * sc["kcol_avg"]
+    tg, tc = eng.tally(0), ora.tally(0)
+    assert tg["generations"] == tc["generations"] == 4
+    assert np.allclose(tg["avg"], tc["avg"], rtol=1e-10, atol=0)
+
+
+def test_fixed_source_matches():
+    b = decks.fixed_source_problem(0, nparticles=3000, precision="fp64")
+    eng, ora, _ = pair(b, nthreads=oracle.cores())
+    sg = eng.run_fixed_source(2, 3000)
+    sc = ora.run_fixed_source(2, 3000)
+    assert sg["collisions"] == sc["collisions"]
+    assert abs(sg["leak_avg"] - sc["leak_avg"]) <= 1e-11 * abs(sc["leak_avg"])
+    assert np.allclose(eng.tally(0)["avg"], ora.tally(0)["avg"], rtol=1e-10, atol=0)
+
+
+@pytest.mark.parametrize("name", ["PUa-1-0-IN", "PUb-1-0-SL", "Ua-1-1-CY"])
+def test_reference_decks_trace_parity(name):
+    b = decks.from_reference_deck(DECKS[name], nparticles=256)
+    eng, ora, _ = pair(b)
+    bank = ora.sample_sources(0, 256)
+    eng.set_trace(128, 1 << 20)
+    ora.set_trace(128, 1 << 20)
+    eng.transport(bank, 1.0, True)
+    ora.transport(bank, 1.0, True)
+    compare_traces(eng.get_trace(), ora.get_trace())
+
+
+@pytest.mark.parametrize("name,precision", [("PUa-1-0-IN", "fp64"), ("PUa-1-0-IN", "mixed"),
+                                            ("PUb-1-0-SL", "mixed")])
+def test_reference_known_answers_on_gpu(name, precision):
+    deck = DECKS[name]
+    eng = Engine(decks.from_reference_deck(deck, nparticles=100000).build(precision=precision), 0)
+    st, _, _ = eng.run_power_iteration(40, 10)
+    assert abs(st["kcol_avg"] - deck["_expected_k"]) < 4 * st["kcol_std"] + 2e-4, st
+
+
+def test_mixed_precision_statistics_config0():
+    """FP32 tracking / FP64 tallies: k within 2 sigma of the FP64 path and at
+    least 95 % of flux bins with |z| < 2."""
+    res = {}
+    for prec in ("fp64", "mixed"):
+        eng = Engine(decks.config0(nparticles=20000).build(precision=prec), 0)
+        st, _, _ = eng.run_power_iteration(40, 10)
+        t = eng.tally(0)
+        g = t["generations"]
+        res[prec] = (st, t["avg"], np.sqrt(t["var"] / g))
+    (s64, a64, e64), (s32, a32, e32) = res["fp64"], res["mixed"]
+    dk = abs(s32["kcol_avg"] - s64["kcol_avg"])
+    assert dk < 2 * np.hypot(s32["kcol_std"], s64["kcol_std"]) + 1e-5, (s32["kcol_avg"], s64["kcol_avg"])
+    m = (e64 > 0) & (e32 > 0)
+    z = (a32[m] - a64[m]) / np.hypot(e32[m], e64[m])
+    assert np.mean(np.abs(z) < 2) >= 0.95
+
+
+def test_errors_leave_the_context_usable():
+    b = decks.config0(nparticles=64)
+    eng, ora, _ = pair(b)
+    bank = ora.sample_sources(0, 64)
+    bad = bank.copy()
+    bad["E"][5] = 99.0  # outside the group structure
+    with pytest.raises(AbxError) as e:
+        eng.transport(bad, 1.0, True)
+    assert e.value.code == 1
+    sg, _ = eng.transport(bank, 1.0, True)
+    sc, _ = ora.transport(bank, 1.0, True)
+    assert np.array_equal(sg["parent_daughter_id"], sc["parent_daughter_id"])
+    with pytest.raises(AbxError):
+        eng.transport(bank, 1.0, True, site_capacity=1)

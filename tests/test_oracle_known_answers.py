@@ -1,0 +1,64 @@
+"""The oracle against the reference's analytic multigroup benchmarks
+(input_files/PU{a,b}-1-0-{IN,SL}.yaml headers) and its own consistency.
+
+These are statistical pins: k within 4 standard deviations of the analytic
+value with a bounded number of histories."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from abeille_gb300 import decks
+
+DECKS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_decks.json")))
+
+
+@pytest.mark.parametrize("name", ["PUa-1-0-IN", "PUb-1-0-IN", "PUa-1-0-SL", "PUb-1-0-SL"])
+def test_analytic_k(name):
+    deck = DECKS[name]
+    built = decks.from_reference_deck(deck, nparticles=20000).build()
+    o = oracle.Oracle(built, nthreads=oracle.cores())
+    st, _, _ = o.run_power_iteration(50, 10)
+    k, s = st["kcol_avg"], st["kcol_std"]
+    assert s > 0
+    assert abs(k - deck["_expected_k"]) < 4 * s + 1e-4, (k, s, deck["_expected_k"])
+
+
+@pytest.mark.parametrize("name", ["Ua-1-1-CY", "UD2O-2-1-SL"])
+def test_delta_and_surface_tracking_agree(name):
+    deck = DECKS[name]
+    ks = []
+    for tr in ("surface-tracking", "delta-tracking"):
+        built = decks.from_reference_deck(deck, nparticles=20000, tracking=tr).build()
+        st, _, _ = oracle.Oracle(built, nthreads=oracle.cores()).run_power_iteration(40, 10)
+        ks.append((st["kcol_avg"], st["kcol_std"]))
+    (k1, s1), (k2, s2) = ks
+    assert abs(k1 - k2) < 4 * np.hypot(s1, s2) + 1e-4, ks
+
+
+def test_thread_count_does_not_change_results():
+    built = decks.config0(nparticles=3000).build()
+    o = oracle.Oracle(built)
+    bank = o.sample_sources(0, 3000)
+    s1, c1 = o.transport(bank, 1.0, True, nthreads=1)
+    t1 = o.tally(0)["gen"].copy()
+    o.clear_generation()
+    s8, c8 = o.transport(bank, 1.0, True, nthreads=8)
+    t8 = o.tally(0)["gen"]
+    assert np.array_equal(s1, s8)
+    assert c1["collisions"] == c8["collisions"]
+    assert np.allclose(t1, t8, rtol=1e-12, atol=0)
+    assert abs(c1["k_col"] - c8["k_col"]) <= 1e-12 * abs(c1["k_col"])
+
+
+def test_bank_order_and_weights():
+    built = decks.config0(nparticles=2000).build()
+    o = oracle.Oracle(built, nthreads=4)
+    bank = o.sample_sources(0, 2000)
+    sites, _ = o.transport(bank, 1.0, False)
+    key = sites["parent_history_id"].astype(np.int64) * 1000 + sites["parent_daughter_id"].astype(np.int64)
+    assert np.all(np.diff(key) > 0)
+    assert set(np.unique(sites["wgt"])) <= {1.0, -1.0}
+    assert np.all((sites["E"] > 0) & (sites["E"] < 7))
