@@ -136,7 +136,7 @@ class TraceRec(C.Structure):
 class GenRecord(C.Structure):
     _fields_ = [("kcol", C.c_double), ("entropy", C.c_double), ("step_ms", C.c_double),
                 ("transport_ms", C.c_double), ("collisions", C.c_uint64), ("flights", C.c_uint64),
-                ("histories", C.c_uint64), ("sites", C.c_uint64)]
+                ("histories", C.c_uint64), ("sites", C.c_uint64), ("lost", C.c_uint64)]
 
 
 # every entry point declared in include/abeille_gb300.h, with its argument types

@@ -24,6 +24,8 @@ template <class R> struct Tol;
 template <> struct Tol<double> {
   static constexpr double INF = DBL_MAX;
   static constexpr double SC = 1e-12;             // SURFACE_COINCIDENT
+  static constexpr double SCD = 1e-12;            // plane on-surface band
+  static constexpr double SCQ = 1e-12;            // quadric on-surface band
   static constexpr double BTOL = 500. * 1e-12;    // BOUNDRY_TOL
   static constexpr double TILE = 100 * 1e-12;     // tile-wall skip
   static constexpr double REL = 1e-14;            // relative distance tie
@@ -32,7 +34,9 @@ template <> struct Tol<double> {
 };
 template <> struct Tol<float> {
   static constexpr float INF = FLT_MAX;
-  static constexpr float SC = 2e-5f;
+  static constexpr float SC = 2e-5f;   // sign ties and lattice-face nudges
+  static constexpr float SCD = 0.f;    // planes: "on surface" only through the surface token
+  static constexpr float SCQ = 1e-6f;  // quadrics: |c| band treated as on-surface
   static constexpr float BTOL = 4e-5f;
   static constexpr float TILE = 4e-5f;
   static constexpr float REL = 1e-6f;
@@ -196,7 +200,7 @@ template <class R> ABX_DEV int surf_sign(const SurfT<R>& s, V3<R> r, V3<R> u) {
 }
 
 template <class R> ABX_DEV R axis_dist(R diff, R ua, bool on) {
-  if (on || m_abs(diff) < Tol<R>::SC || ua == R(0)) return Tol<R>::INF;
+  if (on || m_abs(diff) < Tol<R>::SCD || ua == R(0)) return Tol<R>::INF;
   if (diff / ua < R(0)) return Tol<R>::INF;
   return diff / ua;
 }
@@ -206,7 +210,7 @@ template <class R> ABX_DEV R axis_dist(R diff, R ua, bool on) {
 // FP32 cancellation would dominate.
 template <class R> ABX_DEV R quad_dist(R a, R k, R c, R quad, bool on) {
   if (quad < R(0)) return Tol<R>::INF;
-  if (on || m_abs(c) < Tol<R>::SC) {
+  if (on || m_abs(c) < Tol<R>::SCQ) {
     if (k >= R(0)) return Tol<R>::INF;
     return (-k + m_sqrt(quad)) / a;
   }
@@ -220,7 +224,7 @@ template <class R> ABX_DEV R grazing_fix(R a, R k, R c, bool on) {
   double ad = a, kd = k, cd = c;
   double q = kd * kd - ad * cd;
   if (q < 0.) return Tol<R>::INF;
-  if (on || fabs(cd) < (double)Tol<R>::SC) {
+  if (on || fabs(cd) < (double)Tol<R>::SCQ) {
     if (kd >= 0.) return Tol<R>::INF;
     return (R)((-kd + sqrt(q)) / ad);
   }
@@ -239,7 +243,7 @@ template <class R> ABX_DEV R surf_dist(const SurfT<R>& s, V3<R> r, V3<R> u, bool
       R num = s.c[3] - s.c[0] * r.x - s.c[1] * r.y - s.c[2] * r.z;
       R den = s.c[0] * u.x + s.c[1] * u.y + s.c[2] * u.z;
       R d = num / den;
-      if (on || m_abs(d) < Tol<R>::SC || den == R(0)) return Tol<R>::INF;
+      if (on || m_abs(d) < Tol<R>::SCD || den == R(0)) return Tol<R>::INF;
       if (d < R(0)) return Tol<R>::INF;
       return d;
     }
@@ -439,17 +443,21 @@ ABX_DEV uint32_t pad_pack(int type, int frame, int idx) {
 ABX_DEV int pad_type(uint32_t p) { return (int)(p & 3u); }
 ABX_DEV int pad_frame(uint32_t p) { return (int)((p >> 2) & 3u); }
 ABX_DEV int pad_idx(uint32_t p) { return (int)(p >> 4); }
-ABX_DEV uint64_t tile_pack(const int t[3]) {
-  auto c = [](int v) -> uint64_t {
-    v = v < -1048575 ? -1048575 : (v > 1048575 ? 1048575 : v);
-    return (uint64_t)(uint32_t)(v + 1048576) & 0x1FFFFFull;
+// Tile indices packed as three 10-bit fields, clamped to [-512, 511].  Lattice
+// shapes are limited to 500 per axis, so every in-lattice tile is exact; two
+// out-of-lattice tiles that clamp alike both send a lookup to the outer
+// universe, so the clamp never changes which cell is found.
+ABX_DEV uint32_t tile_pack(const int t[3]) {
+  auto c = [](int v) -> uint32_t {
+    v = v < -512 ? -512 : (v > 511 ? 511 : v);
+    return (uint32_t)(v + 512) & 0x3FFu;
   };
-  return c(t[0]) | (c(t[1]) << 21) | (c(t[2]) << 42);
+  return c(t[0]) | (c(t[1]) << 10) | (c(t[2]) << 20);
 }
-ABX_DEV void tile_unpack(uint64_t p, int t[3]) {
-  t[0] = (int)(p & 0x1FFFFFull) - 1048576;
-  t[1] = (int)((p >> 21) & 0x1FFFFFull) - 1048576;
-  t[2] = (int)((p >> 42) & 0x1FFFFFull) - 1048576;
+ABX_DEV void tile_unpack(uint32_t p, int t[3]) {
+  t[0] = (int)(p & 0x3FFu) - 512;
+  t[1] = (int)((p >> 10) & 0x3FFu) - 512;
+  t[2] = (int)((p >> 20) & 0x3FFu) - 512;
 }
 
 template <class R> struct Trk {
@@ -459,19 +467,13 @@ template <class R> struct Trk {
   int cell;       // material cell, -1 when lost
   int err;        // first error
   uint32_t pad[MAXD];
-  uint64_t tl[MAXD];
+  uint32_t tl[MAXD];
   V3<R> fr[MAXF];
 
   ABX_DEV uint32_t getpad(int k) const {
     uint32_t v = 0;
 #pragma unroll
     for (int i = 0; i < MAXD; i++) if (i == k) v = pad[i];
-    return v;
-  }
-  ABX_DEV uint64_t gettile(int k) const {
-    uint64_t v = 0;
-#pragma unroll
-    for (int i = 0; i < MAXD; i++) if (i == k) v = tl[i];
     return v;
   }
   ABX_DEV V3<R> getfr(int f) const {
@@ -484,7 +486,7 @@ template <class R> struct Trk {
 #pragma unroll
     for (int i = 0; i < MAXF; i++) if (i == f) fr[i] = v;
   }
-  ABX_DEV bool push(uint32_t p, uint64_t t) {
+  ABX_DEV bool push(uint32_t p, uint32_t t) {
     if (depth >= MAXD || pad_frame(p) >= MAXF) {
       err = ABX_ERR_INVALID;
       return false;
@@ -657,6 +659,75 @@ template <class R> ABX_DEV Bound<R> trk_nearest(const Tables& T, const View<R>& 
           b.si = b.token ? b.token - 1 : -1;
           b.btype = b.si >= 0 ? V.surf[b.si].bc : ABX_BC_NORMAL;
           if (b.si >= 0 && surf_sign(V.surf[b.si], rl, k.u) < 0) b.token = -b.token;
+        }
+      }
+    }
+  }
+  return b;
+}
+
+
+// Mixed-mode boundary-condition search, used only after a flight has left the
+// geometry.  Same walk as trk_bc, but an axis plane that the particle is
+// within the FP32 coincidence band of (or just past) while heading through it
+// is at distance 0 rather than ignored: in FP32 that band is ~1e-5 cm wide,
+// not the reference's 1e-12, and ignoring it would pick a far wall.
+template <class R> ABX_DEV R bc_surf_dist(const SurfT<R>& s, V3<R> r, V3<R> u, bool on) {
+  if (sizeof(R) == 4 && !on && s.type <= ABX_SURF_ZPLANE) {
+    R diff = s.type == ABX_SURF_XPLANE ? s.c[0] - r.x : (s.type == ABX_SURF_YPLANE ? s.c[0] - r.y : s.c[0] - r.z);
+    R ua = s.type == ABX_SURF_XPLANE ? u.x : (s.type == ABX_SURF_YPLANE ? u.y : u.z);
+    if (ua == R(0)) return Tol<R>::INF;
+    R d = diff / ua;
+    if (d >= R(0)) return d;
+    return m_abs(diff) < Tol<R>::SC ? R(0) : Tol<R>::INF;
+  }
+  return surf_dist(s, r, u, on);
+}
+
+template <class R>
+ABX_DEV Bound<R> cells_bc_mixed(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<R> u, int32_t on, Bound<R> b) {
+  const CellT c = T.cells[ci];
+  if (!c.has_bc) return b;
+  const int32_t* __restrict__ rpn = T.rpn + c.rpn_off;
+  R mind = Tol<R>::INF;
+  int32_t is = 0;
+  for (int i = 0; i < c.rpn_len; i++) {
+    int32_t t = __ldg(rpn + i);
+    if (t >= ABX_OP_UNIN) continue;
+    const SurfT<R> s = V.surf[abs(t) - 1];
+    if (s.bc == ABX_BC_NORMAL) continue;
+    R d = bc_surf_dist(s, r, u, abs(t) == abs(on));
+    if (d < mind) { mind = d; is = -t; }
+  }
+  if (is != 0 && mind < b.dist) {
+    int32_t tmp = abs(is);
+    b.dist = mind; b.token = tmp; b.si = tmp - 1;
+    b.btype = V.surf[b.si].bc;
+  }
+  return b;
+}
+
+template <class R> ABX_DEV Bound<R> trk_bc_mixed(const Tables& T, const View<R>& V, const ProbT& P, const Trk<R>& k) {
+  Bound<R> b{Tol<R>::INF, -1, ABX_BC_VACUUM, 0};
+#pragma unroll
+  for (int i = 0; i < MAXD; i++) {
+    if (i < k.depth) {
+      uint32_t p = k.pad[i];
+      int ty = pad_type(p), id = pad_idx(p);
+      V3<R> rl = k.getfr(pad_frame(p));
+      if (ty == PAD_CELL) {
+        b = cells_bc_mixed(T, V, id, rl, k.u, k.token, b);
+      } else if (T.univ[id].has_bc) {
+        int ui = id;
+        for (int guard = 0; guard < 16; guard++) {
+          const UnivT U = T.univ[ui];
+          if (U.kind == ABX_UNIV_RECT_LATTICE) {
+            if (!U.has_bc) break;
+            ui = U.outer;
+            continue;
+          }
+          for (int j = 0; j < U.list_len; j++) b = cells_bc_mixed(T, V, __ldg(T.cell_lists + U.list_off + j), rl, k.u, k.token, b);
+          break;
         }
       }
     }

@@ -242,8 +242,8 @@ static int append_problem(Pools& P, const abx_problem* pr) {
       if (u.shape[0] <= 0 || u.shape[1] <= 0 || u.shape[2] <= 0 || n != u.list_len ||
           u.list_offset < 0 || u.list_offset + n > pr->n_lattice_elems)
         return fail(ABX_ERR_INVALID, "lattice %u: shape/elements mismatch", u.id);
-      if (u.shape[0] > 1000000 || u.shape[1] > 1000000 || u.shape[2] > 1000000)
-        return fail(ABX_ERR_INVALID, "lattice %u: too many tiles along an axis", u.id);
+      if (u.shape[0] > 500 || u.shape[1] > 500 || u.shape[2] > 500)
+        return fail(ABX_ERR_UNSUPPORTED, "lattice %u: more than 500 tiles along an axis", u.id);
       t.list_off = (int)P.lat_elems.size();
       t.list_len = (int)n;
       for (int a = 0; a < 3; a++) t.n[a] = u.shape[a];
@@ -844,6 +844,7 @@ __global__ void k_gen_end(DevState* st, RunAcc* run, const ProbT* probs, abx_gen
     r.flights = st->flights;
     r.histories = st->n_hist;
     r.sites = st->site_count;
+    r.lost = st->lost;
   }
   run->total_coll += st->collisions;
   run->total_flights += st->flights;

@@ -71,15 +71,19 @@ template <> ABX_DEV void tally_geom<float>(const TallyT& t, float low[3], float 
   for (int a = 0; a < 3; a++) { low[a] = t.lowf[a]; hi[a] = t.hif[a]; d[a] = t.df[a]; dinv[a] = t.dinvf[a]; }
 }
 
-// Per-lane score accumulators.  FP64 mode sums each term in double as the
-// reference's ThreadLocalScores does; the mixed mode sums a history's terms in
-// float and adds the history total to a double accumulator.
+// Score accumulators.  Each history sums its terms in the tracking precision;
+// at the end of the history the five totals are added, in FP64, to the block's
+// shared accumulators (one FP64 atomic each), which the block adds to the
+// global scores when it retires.  In FP64 mode every term is a double, so
+// the sums are FP64 throughout, as the reference's ThreadLocalScores.
 template <class R> struct Acc {
-  double kcol = 0, kabs = 0, ktrk = 0, leak = 0, mig = 0;
   R hcol = 0, habs = 0, htrk = 0, hleak = 0, hmig = 0;
-  ABX_DEV void flush() {
-    kcol += (double)hcol; kabs += (double)habs; ktrk += (double)htrk;
-    leak += (double)hleak; mig += (double)hmig;
+  ABX_DEV void flush(double* sh) {
+    atomicAdd(sh + 0, (double)hcol);
+    atomicAdd(sh + 1, (double)habs);
+    atomicAdd(sh + 2, (double)htrk);
+    atomicAdd(sh + 3, (double)hleak);
+    atomicAdd(sh + 4, (double)hmig);
     hcol = habs = htrk = hleak = hmig = R(0);
   }
 };
@@ -89,13 +93,12 @@ template <class R> struct Lane {
   R E, w, w2;
   int g;
   uint64_t rng;
-  uint64_t hid, fam;
   uint32_t h;
   int pid;
   int mat;
   uint32_t dau;
   uint32_t nsec;
-  uint64_t events;
+  uint32_t events;
   uint32_t npos, nneg;
 };
 
@@ -363,7 +366,7 @@ ABX_DEV void collide(const TransportArgs<R>& A, const Tables& T, const View<R>& 
           sp[6] = E_out; sp[7] = wgt; sp[8] = R(0);
           L.nsec++;
         } else {
-          raise_err(A.st, ABX_ERR_CAPACITY, L.hid);
+          raise_err(A.st, ABX_ERR_CAPACITY, L.h);
           atomicAdd(&A.st->sec_overflow, 1ull);
         }
       }
@@ -405,13 +408,23 @@ ABX_DEV void do_reflection(const Tables& T, const View<R>& V, const ProbT& P, Tr
   // cleared by set_r, and previous-position bookkeeping only feeds cancellation.
   const SurfT<R> s = V.surf[b.si];
   V3<R> r_on = add(L.r, scl(L.u, b.dist));
+  if (sizeof(R) == 4) {  // mixed mode: put the point exactly on an axis plane
+    if (s.type == ABX_SURF_XPLANE) r_on.x = s.c[0];
+    else if (s.type == ABX_SURF_YPLANE) r_on.y = s.c[0];
+    else if (s.type == ABX_SURF_ZPLANE) r_on.z = s.c[0];
+  }
   V3<R> n = surf_norm(s, r_on);
   R c2 = R(2) * dot(L.u, n);
   V3<R> nd = sub(L.u, scl(n, c2));
+  // the side token the reference computes before set_r clears it
+  const int32_t side = surf_sign(s, L.r, L.u) < 0 ? -(b.si + 1) : (b.si + 1);
   L.r = r_on;
   L.u = dir3(nd.x, nd.y, nd.z);
   trk_set_r(k, L.r);
   k.u = L.u;
+  // Mixed mode keeps it: the particle sits on the plane, and with no FP32
+  // distance band the token is what marks that plane as the one it is on.
+  if (sizeof(R) == 4) k.token = side;
   trk_restart(T, V, P, k);
 }
 
@@ -426,8 +439,6 @@ ABX_DEV bool lane_load(const TransportArgs<R>& A, const Tables& T, const View<R>
   L.w = A.bank.w[h];
   L.w2 = A.bank.w2 ? A.bank.w2[h] : R(0);
   L.rng = A.bank.rng[h];
-  L.hid = A.bank.hid[h];
-  L.fam = A.bank.fam ? A.bank.fam[h] : 0;
   L.pid = A.bank.prob ? A.bank.prob[h] : 0;
   L.rb = L.r;
   L.dau = 0;
@@ -451,7 +462,7 @@ ABX_DEV bool lane_load(const TransportArgs<R>& A, const Tables& T, const View<R>
 }
 
 template <class R, int TRACK>
-__global__ void __launch_bounds__(256, 1) transport_kernel(const TransportArgs<R> A) {
+__global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R> A) {
   const bool TRACE = A.trace != nullptr;
   const Tables& T = A.T;
   const View<R> V = make_view<R>(T);
@@ -461,10 +472,14 @@ __global__ void __launch_bounds__(256, 1) transport_kernel(const TransportArgs<R
   const R kcol = (R)st->kcol;
   const bool converged = st->converged != 0;
 
+  __shared__ double sh_acc[5];
+  if (threadIdx.x < 5) sh_acc[threadIdx.x] = 0.;
+  __syncthreads();
+
   Lane<R> L;
   Trk<R> k;
   Acc<R> acc;
-  unsigned long long ncoll = 0, nflight = 0, nlost = 0;
+  uint32_t ncoll = 0, nflight = 0, nlost = 0;
   bool active = false, done = false;
   L.h = 0xffffffffu;
   L.pid = 0;
@@ -490,7 +505,7 @@ __global__ void __launch_bounds__(256, 1) transport_kernel(const TransportArgs<R
           done = true;
         } else {
           active = lane_load(A, T, V, L, k, (uint32_t)h);
-          if (k.err) { raise_err(st, k.err, L.hid); done = true; active = false; }
+          if (k.err) { raise_err(st, k.err, L.h); done = true; active = false; }
           else if (!active) {
             nlost++;
             A.hist_count[h] = 0;
@@ -517,7 +532,10 @@ __global__ void __launch_bounds__(256, 1) transport_kernel(const TransportArgs<R
       if (k.cell < 0) {
         trk_set_r(k, L.r);
         trk_current(T, V, P, k);
-        bound = trk_bc(T, V, P, k);
+        // Mixed mode: the search is direction-aware at axis planes, so a
+        // particle within the FP32 coincidence band of the wall it leaves
+        // through finds that wall (trk_bc_mixed).
+        bound = sizeof(R) == 8 ? trk_bc(T, V, P, k) : trk_bc_mixed(T, V, P, k);
         crossed = true;
       }
       if (converged && P.has_tle) score_flight(T, V, P, L, d_coll < bound.dist ? d_coll : bound.dist);
@@ -531,18 +549,23 @@ __global__ void __launch_bounds__(256, 1) transport_kernel(const TransportArgs<R
           if (TRACE) trace_rec(A, L, 2, k.cell);
         } else if (bound.btype == ABX_BC_REFLECTIVE) {
           do_reflection(T, V, P, k, L, bound);
-          if (k.cell < 0) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.hid); done = true; active = false; continue; }
+          if (k.cell < 0) {
+            if (sizeof(R) == 8) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
+            nlost++;  // mixed mode: counted in `lost` and killed
+            alive = false;
+          }
           if (TRACE) trace_rec(A, L, 3, k.cell);
         } else {
-          raise_err(st, ABX_ERR_LOST_PARTICLE, L.hid);
-          done = true; active = false; continue;
+          if (sizeof(R) == 8) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
+          nlost++;
+          alive = false;
         }
       } else {
         L.r = add(L.r, scl(L.u, d_coll));
         L.mat = T.cells[k.cell].fill;
         const MatT& M = T.mats[L.mat];
         const R Et = V.xs[M.xs_off + XS_ET * M.G + L.g];
-        if (Et - Emaj > Tol<R>::MAJ) { raise_err(st, ABX_ERR_MAJORANT, L.hid); done = true; active = false; continue; }
+        if (Et - Emaj > Tol<R>::MAJ) { raise_err(st, ABX_ERR_MAJORANT, L.h); done = true; active = false; continue; }
         if (canon<R>(L.rng) < (Et / Emaj)) had_collision = true;
         if (TRACE) trace_rec(A, L, had_collision ? 1 : 0, k.cell);
       }
@@ -564,14 +587,14 @@ __global__ void __launch_bounds__(256, 1) transport_kernel(const TransportArgs<R
           if (TRACE) trace_rec(A, L, 2, k.cell);
         } else if (bound.btype == ABX_BC_REFLECTIVE) {
           do_reflection(T, V, P, k, L, bound);
-          if (k.cell < 0) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.hid); done = true; active = false; continue; }
+          if (k.cell < 0) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
           if (TRACE) trace_rec(A, L, 3, k.cell);
         } else {
           trk_move(k, bound.dist);
           k.token = -bound.token;
           trk_current(T, V, P, k);
           L.r = add(L.r, scl(L.u, bound.dist));
-          if (k.cell < 0) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.hid); done = true; active = false; continue; }
+          if (k.cell < 0) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
           L.mat = T.cells[k.cell].fill;
           if (TRACE) trace_rec(A, L, 5, k.cell);
         }
@@ -582,7 +605,7 @@ __global__ void __launch_bounds__(256, 1) transport_kernel(const TransportArgs<R
         if (TRACE) trace_rec(A, L, 1, k.cell);
       }
     }
-    if (k.err) { raise_err(st, k.err, L.hid); done = true; active = false; continue; }
+    if (k.err) { raise_err(st, k.err, L.h); done = true; active = false; continue; }
     if (alive && had_collision) {
       ncoll++;
       collide(A, T, V, P, L, acc, converged, kcol, alive);
@@ -599,41 +622,40 @@ __global__ void __launch_bounds__(256, 1) transport_kernel(const TransportArgs<R
         L.u = mk<R>(sp[3], sp[4], sp[5]);
         L.E = sp[6]; L.w = sp[7]; L.w2 = sp[8];
         L.g = group_of<R>(V.ebnd + P.eb_off, P.G, L.E);
-        if (L.g >= P.G) { raise_err(st, ABX_ERR_INVALID, L.hid); done = true; active = false; continue; }
+        if (L.g >= P.G) { raise_err(st, ABX_ERR_INVALID, L.h); done = true; active = false; continue; }
         trk_set_r(k, L.r);
         k.u = L.u;
         trk_restart(T, V, P, k);
-        if (k.cell < 0 || k.err) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.hid); done = true; active = false; continue; }
+        if (k.cell < 0 || k.err) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
         L.mat = T.cells[k.cell].fill;
         if (TRACE) trace_rec(A, L, 6, k.cell);
       } else {
         A.hist_count[L.h] = L.dau;
-        acc.flush();
+        acc.flush(sh_acc);
         active = false;
       }
     } else if (L.events > A.max_events) {
-      raise_err(st, ABX_ERR_TIMEOUT, L.hid);
+      raise_err(st, ABX_ERR_TIMEOUT, L.h);
       done = true;
       active = false;
     }
   }
-  acc.flush();
-  // block reduction of the scores
-  double v[5] = {acc.kcol, acc.kabs, acc.ktrk, acc.leak, acc.mig};
+  acc.flush(sh_acc);
   unsigned long long c[5] = {ncoll, nflight, nlost, (unsigned long long)L.npos, (unsigned long long)L.nneg};
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
-    for (int i = 0; i < 5; i++) v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
-#pragma unroll
     for (int i = 0; i < 5; i++) c[i] += __shfl_down_sync(0xffffffffu, c[i], o);
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(&st->scores[0], sh_acc[0]);
+    atomicAdd(&st->scores[1], sh_acc[1]);
+    atomicAdd(&st->scores[2], sh_acc[2]);
+    atomicAdd(&st->scores[4], sh_acc[3]);
+    atomicAdd(&st->scores[5], sh_acc[4]);
+  }
   if (lane == 0) {
-    atomicAdd(&st->scores[0], v[0]);
-    atomicAdd(&st->scores[1], v[1]);
-    atomicAdd(&st->scores[2], v[2]);
-    atomicAdd(&st->scores[4], v[3]);
-    atomicAdd(&st->scores[5], v[4]);
     atomicAdd(&st->collisions, c[0]);
     atomicAdd(&st->flights, c[1]);
     atomicAdd(&st->lost, c[2]);

@@ -260,7 +260,7 @@ def main():
         "gpu_launches": KERNELS_PER_GEN * args.steps,
         "clocks": clk.summary(),
         "detail": {"flights": flights, "collisions": coll, "sites": sites, "transport_ms": tr_ms,
-                   "wall_s": wall, "kcol_last": recs[-1]["kcol"]},
+                   "wall_s": wall, "kcol_last": recs[-1]["kcol"], "lost": sum(r["lost"] for r in recs)},
     }
     print(json.dumps(line), flush=True)
     if dist:

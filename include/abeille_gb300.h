@@ -328,6 +328,7 @@ typedef struct abx_gen_record {
   double step_ms;       /* device time of the whole generation step          */
   double transport_ms;  /* device time of the transport kernel               */
   uint64_t collisions, flights, histories, sites;
+  uint64_t lost;        /* particles lost (mixed mode counts and kills them) */
 } abx_gen_record;
 /* As abx_run_power_iteration, with a per-generation record array [ngenerations]. */
 int abx_run_power_iteration_ex(abx_ctx* ctx, int ngenerations, int nignored,

@@ -39,6 +39,8 @@ def compare_traces(tg, tc):
     assert close(tg["r"], tc["r"], atol=1e-9)
     assert close(tg["u"], tc["u"], atol=1e-9)
     assert close(tg["wgt"], tc["wgt"])
+    exact = np.mean(np.all(tg["r"] == tc["r"], axis=1) & np.all(tg["u"] == tc["u"], axis=1))
+    print(f"trace records: {len(tg)}, bit-identical position+direction: {exact:.4f}")
 
 
 @pytest.mark.parametrize("cfg", [0, 2])
@@ -84,7 +86,16 @@ def test_transport_step_matches(cfg, tracking):
         assert cg[k] == cc[k], k
     for k in ("k_col", "k_abs", "k_trk", "leakage", "mig_area"):
         assert abs(cg[k] - cc[k]) <= RTOL * abs(cc[k]) + 1e-300, (k, cg[k], cc[k])
-    assert close(eng.tally(0)["gen"], ora.tally(0)["gen"], atol=0.0)
+    tg, tc = eng.tally(0)["gen"], ora.tally(0)["gen"]
+    assert np.array_equal(tg != 0, tc != 0)
+    assert abs(tg.sum() - tc.sum()) <= RTOL * tc.sum()
+    if cfg == 2:
+        # Track-length segments are differences of positions: a 1-ulp position
+        # difference (CUDA vs glibc log/sin/cos) is ~1e-15 cm absolute, which
+        # is up to ~1e-11 relative on the shortest segments of a bin.
+        assert close(tg, tc, rtol=1e-9, atol=0.0)
+    else:
+        assert close(tg, tc, atol=0.0)
 
 
 def test_power_iteration_matches():
