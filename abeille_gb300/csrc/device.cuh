@@ -667,41 +667,110 @@ template <class R> ABX_DEV Bound<R> trk_nearest(const Tables& T, const View<R>& 
 }
 
 
-// Mixed-mode boundary-condition search, used only after a flight has left the
-// geometry.  Same walk as trk_bc, but an axis plane that the particle is
-// within the FP32 coincidence band of (or just past) while heading through it
-// is at distance 0 rather than ignored: in FP32 that band is ~1e-5 cm wide,
-// not the reference's 1e-12, and ignoring it would pick a far wall.
-template <class R> ABX_DEV R bc_surf_dist(const SurfT<R>& s, V3<R> r, V3<R> u, bool on) {
-  if (sizeof(R) == 4 && !on && s.type <= ABX_SURF_ZPLANE) {
-    R diff = s.type == ABX_SURF_XPLANE ? s.c[0] - r.x : (s.type == ABX_SURF_YPLANE ? s.c[0] - r.y : s.c[0] - r.z);
-    R ua = s.type == ABX_SURF_XPLANE ? u.x : (s.type == ABX_SURF_YPLANE ? u.y : u.z);
-    if (ua == R(0)) return Tol<R>::INF;
-    R d = diff / ua;
-    if (d >= R(0)) return d;
-    return m_abs(diff) < Tol<R>::SC ? R(0) : Tol<R>::INF;
+// ------------------------------------------------- mixed-mode exit distances
+// FP32 positions carry ~1e-6 relative error, so the reference's 1e-12
+// "on the surface" bands cannot be reproduced.  The mixed mode measures, for
+// each half-space of the current cell (region token t: t > 0 is the side where
+// the surface function is positive), the distance along u until the particle
+// leaves that half-space: infinite when moving inward or parallel, clamped to
+// 0 when the point is already (within rounding) on the far side.  This needs
+// no tolerance and cannot pick a wall the particle is moving away from.
+template <class R> ABX_DEV R exit_dist(const SurfT<R>& s, int32_t t, V3<R> r, V3<R> u) {
+  const R INF = Tol<R>::INF;
+  if (s.type <= ABX_SURF_PLANE) {
+    R eval = surf_eval(s, r);
+    R rate = s.type == ABX_SURF_XPLANE ? u.x
+             : s.type == ABX_SURF_YPLANE ? u.y
+             : s.type == ABX_SURF_ZPLANE ? u.z
+                                         : s.c[0] * u.x + s.c[1] * u.y + s.c[2] * u.z;
+    bool exiting = t > 0 ? rate < R(0) : rate > R(0);
+    if (!exiting) return INF;
+    R d = -eval / rate;
+    return d > R(0) ? d : R(0);
   }
-  return surf_dist(s, r, u, on);
+  R p, q, w = R(0), up, uq, uw = R(0), Rr;
+  if (s.type == ABX_SURF_SPHERE) {
+    p = r.x - s.c[0]; q = r.y - s.c[1]; w = r.z - s.c[2]; up = u.x; uq = u.y; uw = u.z; Rr = s.c[3];
+  } else if (s.type == ABX_SURF_ZCYLINDER) {
+    p = r.y - s.c[1]; q = r.x - s.c[0]; up = u.y; uq = u.x; Rr = s.c[2];
+  } else if (s.type == ABX_SURF_XCYLINDER) {
+    p = r.y - s.c[0]; q = r.z - s.c[1]; up = u.y; uq = u.z; Rr = s.c[2];
+  } else {
+    p = r.x - s.c[0]; q = r.z - s.c[1]; up = u.x; uq = u.z; Rr = s.c[2];
+  }
+  const R a = up * up + uq * uq + uw * uw;
+  const R k = p * up + q * uq + w * uw;
+  const R c = p * p + q * q + w * w - Rr * Rr;
+  if (a == R(0)) return ((t < 0) == (c > R(0))) ? R(0) : INF;
+  // roots of a s^2 + 2 k s + c = 0; FP64 when the discriminant is small
+  // against k^2 (grazing incidence), where FP32 cancellation would dominate
+  double ad = a, kd = k, cd = c;
+  double quad = kd * kd - ad * cd;
+  if (t < 0) {  // inside: leave through the far root
+    if (c > R(0) && k >= R(0)) return R(0);
+    if (quad < 0.) return R(0);
+    double d = (-kd + sqrt(quad)) / ad;
+    return d > 0. ? (R)d : R(0);
+  }
+  if (c < R(0)) return R(0);  // outside region but within the quadric
+  if (k >= R(0) || quad < 0.) return INF;
+  double d = (-kd - sqrt(quad)) / ad;
+  return d > 0. ? (R)d : R(0);
 }
 
+// Distance to leave a simple cell (intersection of half-spaces); for a cell
+// with unions or complements the reference's per-surface distances are used.
 template <class R>
-ABX_DEV Bound<R> cells_bc_mixed(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<R> u, int32_t on, Bound<R> b) {
+ABX_DEV void cell_exit(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<R> u, int32_t on, bool bc_only,
+                       R& dist, int32_t& isurf) {
   const CellT c = T.cells[ci];
-  if (!c.has_bc) return b;
-  const int32_t* __restrict__ rpn = T.rpn + c.rpn_off;
+  if (!c.simple) {
+    cell_dist(T, V, ci, r, u, on, bc_only, dist, isurf);
+    return;
+  }
   R mind = Tol<R>::INF;
   int32_t is = 0;
+  const int32_t* __restrict__ rpn = T.rpn + c.rpn_off;
   for (int i = 0; i < c.rpn_len; i++) {
     int32_t t = __ldg(rpn + i);
-    if (t >= ABX_OP_UNIN) continue;
     const SurfT<R> s = V.surf[abs(t) - 1];
-    if (s.bc == ABX_BC_NORMAL) continue;
-    R d = bc_surf_dist(s, r, u, abs(t) == abs(on));
+    if (bc_only && s.bc == ABX_BC_NORMAL) continue;
+    R d = exit_dist(s, t, r, u);
     if (d < mind) { mind = d; is = -t; }
   }
-  if (is != 0 && mind < b.dist) {
-    int32_t tmp = abs(is);
-    b.dist = mind; b.token = tmp; b.si = tmp - 1;
+  dist = mind;
+  isurf = is;
+}
+
+// Distance to leave the current lattice tile in the direction of motion.
+template <class R> ABX_DEV R tile_exit(const LatT<R>& L, V3<R> rl, V3<R> u, const int t[3]) {
+  V3<R> rt = sub(rl, tile_center(L, t[0], t[1], t[2]));
+  const R h[3] = {L.p[0] * R(0.5), L.p[1] * R(0.5), L.p[2] * R(0.5)};
+  const R x[3] = {rt.x, rt.y, rt.z}, v[3] = {u.x, u.y, u.z};
+  R dist = Tol<R>::INF;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    if (v[a] == R(0)) continue;
+    R d = ((v[a] > R(0) ? h[a] : -h[a]) - x[a]) / v[a];
+    d = d > R(0) ? d : R(0);
+    if (d < dist) dist = d;
+  }
+  return dist;
+}
+
+// Mixed-mode boundary-condition search (used after a flight has left the
+// geometry) and nearest-boundary search (surface tracking): the reference's
+// walks over the tree, with exit distances in place of the banded ones.
+template <class R>
+ABX_DEV Bound<R> cells_bc_mixed(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<R> u, int32_t on, Bound<R> b) {
+  if (!T.cells[ci].has_bc) return b;
+  R d;
+  int32_t is;
+  cell_exit(T, V, ci, r, u, on, true, d, is);
+  if (is != 0 && d < b.dist) {
+    b.dist = d;
+    b.si = abs(is) - 1;
+    b.token = -is;  // the cell's own side of the surface
     b.btype = V.surf[b.si].bc;
   }
   return b;
@@ -728,6 +797,34 @@ template <class R> ABX_DEV Bound<R> trk_bc_mixed(const Tables& T, const View<R>&
           }
           for (int j = 0; j < U.list_len; j++) b = cells_bc_mixed(T, V, __ldg(T.cell_lists + U.list_off + j), rl, k.u, k.token, b);
           break;
+        }
+      }
+    }
+  }
+  return b;
+}
+
+template <class R> ABX_DEV Bound<R> trk_nearest_mixed(const Tables& T, const View<R>& V, const ProbT& P, const Trk<R>& k) {
+  Bound<R> b = trk_bc_mixed(T, V, P, k);
+#pragma unroll
+  for (int i = 0; i < MAXD; i++) {
+    if (i < k.depth) {
+      uint32_t p = k.pad[i];
+      int ty = pad_type(p), id = pad_idx(p);
+      V3<R> rl = k.getfr(pad_frame(p));
+      if (ty == PAD_LATT) {
+        int t[3];
+        tile_unpack(k.tl[i], t);
+        R d = tile_exit(V.lat[T.univ[id].lat], rl, k.u, t);
+        if (d < b.dist) { b.dist = d; b.btype = ABX_BC_NORMAL; b.si = -1; b.token = 0; }
+      } else if (ty == PAD_CELL) {
+        R d; int32_t ts;
+        cell_exit(T, V, id, rl, k.u, k.token, false, d, ts);
+        if (d < b.dist) {
+          b.dist = d;
+          b.token = -ts;  // the cell's own side: crossing flips it
+          b.si = ts ? abs(ts) - 1 : -1;
+          b.btype = b.si >= 0 ? V.surf[b.si].bc : ABX_BC_NORMAL;
         }
       }
     }

@@ -417,7 +417,8 @@ ABX_DEV void do_reflection(const Tables& T, const View<R>& V, const ProbT& P, Tr
   R c2 = R(2) * dot(L.u, n);
   V3<R> nd = sub(L.u, scl(n, c2));
   // the side token the reference computes before set_r clears it
-  const int32_t side = surf_sign(s, L.r, L.u) < 0 ? -(b.si + 1) : (b.si + 1);
+  const int32_t side = sizeof(R) == 4 && b.token != 0 ? b.token
+                       : (surf_sign(s, L.r, L.u) < 0 ? -(b.si + 1) : (b.si + 1));
   L.r = r_on;
   L.u = dir3(nd.x, nd.y, nd.z);
   trk_set_r(k, L.r);
@@ -573,7 +574,7 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
       const MatT& M = T.mats[L.mat];
       const R Et = V.xs[M.xs_off + XS_ET * M.G + L.g];
       R d_coll = Et == R(0) ? Tol<R>::INF : -m_log(R(1) - canon<R>(L.rng)) / Et;
-      Bound<R> bound = trk_nearest(T, V, P, k);
+      Bound<R> bound = sizeof(R) == 8 ? trk_nearest(T, V, P, k) : trk_nearest_mixed(T, V, P, k);
       R dmin = d_coll < bound.dist ? d_coll : bound.dist;
       if (converged && P.has_tle) score_flight(T, V, P, L, dmin);
       acc.htrk += L.w * dmin * V.xs[M.xs_off + XS_VEF * M.G + L.g];
@@ -587,15 +588,31 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
           if (TRACE) trace_rec(A, L, 2, k.cell);
         } else if (bound.btype == ABX_BC_REFLECTIVE) {
           do_reflection(T, V, P, k, L, bound);
-          if (k.cell < 0) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
+          if (k.cell < 0) {
+            if (sizeof(R) == 8) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
+            nlost++;  // mixed mode: counted in `lost` and killed
+            alive = false;
+          }
           if (TRACE) trace_rec(A, L, 3, k.cell);
         } else {
+          const int prev = k.cell;
           trk_move(k, bound.dist);
           k.token = -bound.token;
           trk_current(T, V, P, k);
           L.r = add(L.r, scl(L.u, bound.dist));
-          if (k.cell < 0) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
-          L.mat = T.cells[k.cell].fill;
+          if (sizeof(R) == 4 && (k.cell < 0 || (k.cell == prev && bound.dist == R(0)))) {
+            // mixed mode: step off a surface crossing FP32 cannot resolve
+            L.r = add(L.r, scl(L.u, R(4) * Tol<R>::SC));
+            trk_set_r(k, L.r);
+            trk_restart(T, V, P, k);
+          }
+          if (k.cell < 0) {
+            if (sizeof(R) == 8) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
+            nlost++;
+            alive = false;
+          } else {
+            L.mat = T.cells[k.cell].fill;
+          }
           if (TRACE) trace_rec(A, L, 5, k.cell);
         }
       } else {
@@ -634,6 +651,13 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
         acc.flush(sh_acc);
         active = false;
       }
+    } else if (sizeof(R) == 4 && L.events > 100000u) {
+      // mixed mode: a history this long is a geometry rounding trap, not
+      // physics; it is counted in `lost` and ended
+      nlost++;
+      A.hist_count[L.h] = L.dau;
+      acc.flush(sh_acc);
+      active = false;
     } else if (L.events > A.max_events) {
       raise_err(st, ABX_ERR_TIMEOUT, L.h);
       done = true;
