@@ -11,7 +11,8 @@ bounded by the boundary-condition surfaces.
   config0  17x17 pin lattice, pitch 1.26, fuel radius 0.54, reflective x/y,
            infinite in z; fuel + moderator, 7 groups; k-eigenvalue, delta
            tracking; 17x17x1 collision flux tally.
-  config1  51x51 pins, 200 cm tall in 10 axial zones bounded by z-planes,
+  config1  51x51 pins, 200 cm tall in 10 axial zones bounded by z-planes
+           (root universe of 10 zone cells, each filled with a 51x51 lattice),
            vacuum top/bottom, reflective sides, a 5x5 water-gap box in the
            centre; 7 groups; 51x51x20 collision flux tally.
   config2  17x17 pins with fuel/gap/clad rings (r = 0.41/0.42/0.475), 8 fuel
@@ -120,34 +121,39 @@ def config1(nparticles=1000000, precision="fp64", tracking="delta-tracking"):
     b.material(1, **fuel)
     b.material(2, **mod)
     b.material(3, **water)
+    # pins: fuel cylinder in moderator; water-gap tiles: one water cell
     b.surface("zcylinder", 1, x0=0.0, y0=0.0, r=0.54)
-    zs = [-100.0 + 20.0 * k for k in range(1, 10)]  # 9 internal planes -> 10 zones
-    for k, z in enumerate(zs):
-        b.surface("zplane", 10 + k, z0=z)
-    pin_cells = []
-    for zone in range(10):
-        lo = f" & +{10 + zone - 1}" if zone > 0 else ""
-        hi = f" & -{10 + zone}" if zone < 9 else ""
-        b.cell(1 + zone, "-1" + lo + hi, material=1)
-        pin_cells.append(1 + zone)
-    for zone in range(10):
-        lo = f" & +{10 + zone - 1}" if zone > 0 else ""
-        hi = f" & -{10 + zone}" if zone < 9 else ""
-        b.cell(20 + zone, "+1" + lo + hi, material=2)
-        pin_cells.append(20 + zone)
     b.surface("zcylinder", 2, x0=0.0, y0=0.0, r=100.0)
-    b.cell(50, "-2", material=3)
-    b.cell(51, "+2", material=3)
+    b.cell(1, "-1", material=1)
+    b.cell(2, "+1", material=2)
+    b.cell(3, "-2", material=3)
+    b.cell_universe(1, [1, 2])
+    b.cell_universe(2, [3])
     half = 51 * PITCH / 2
-    outer = _box_outer(b, half, half, -100.0, 100.0, mat=2)
-    b.cell_universe(1, pin_cells)
-    b.cell_universe(2, [50, 51])
+    # boundary planes: reflective sides, vacuum top and bottom
+    b.surface("xplane", 101, x0=-half, boundary="reflective")
+    b.surface("xplane", 102, x0=half, boundary="reflective")
+    b.surface("yplane", 103, y0=-half, boundary="reflective")
+    b.surface("yplane", 104, y0=half, boundary="reflective")
+    zs = [-100.0 + 20.0 * k for k in range(11)]  # 11 planes bound 10 axial zones
+    for k, z in enumerate(zs):
+        b.surface("zplane", 110 + k, z0=z, boundary="vacuum" if k in (0, 10) else "normal")
     tiles = []
     for i in range(51):        # yaml order: nx runs down the list, ny fastest
         for j in range(51):
             tiles.append(2 if (abs(i - 25) <= 2 and abs(j - 25) <= 2) else 1)
-    b.rect_lattice(10, [51, 51, 1], [PITCH, PITCH, 200.0], [0.0, 0.0, 0.0], tiles, outer=outer)
-    b.set_root(10)
+    # root: one cell per axial zone, bounded by z-planes, each filled with its
+    # own copy of the 51x51 lattice.  The lattice copy takes the zone cell's
+    # id, so the reference's re-descent by the cell pad's id
+    # (universe_id_to_indx[tree.back().id]) lands on that lattice.
+    zone_cells = []
+    for zone in range(10):
+        cid = 200 + zone
+        b.rect_lattice(cid, [51, 51, 1], [PITCH, PITCH, 20.0], [0.0, 0.0, zs[zone] + 10.0], tiles)
+        b.cell(cid, f"+101 & -102 & +103 & -104 & +{110 + zone} & -{111 + zone}", universe=cid)
+        zone_cells.append(cid)
+    b.cell_universe(300, zone_cells)
+    b.set_root(300)
     b.mesh_tally([51, 51, 20], [-half, -half, -100.0], [half, half, 100.0], "collision", "flux", [0.0, 7.0])
     b.set_entropy([-half, -half, -100.0], [half, half, 100.0], [17, 17, 10])
     b.source("box", low=[-half, -half, -100.0], hi=[half, half, 100.0], energy=0.5, fissile_only=True)

@@ -47,7 +47,7 @@ def test_universe_creation_order_matches_reference_parser():
 def test_built_struct_counts():
     built = decks.config1(nparticles=10).build()
     p = built.struct
-    assert p.n_universes == 4 and p.n_cells == 23 and p.n_materials == 3
+    assert p.n_universes == 13 and p.n_cells == 13 and p.n_materials == 3
     assert p.settings.ngroups == 7 and p.n_tallies == 1
 
 
