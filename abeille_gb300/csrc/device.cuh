@@ -476,6 +476,12 @@ template <class R> struct Trk {
     for (int i = 0; i < MAXD; i++) if (i == k) v = pad[i];
     return v;
   }
+  ABX_DEV uint32_t gettile(int k) const {
+    uint32_t v = 0;
+#pragma unroll
+    for (int i = 0; i < MAXD; i++) if (i == k) v = tl[i];
+    return v;
+  }
   ABX_DEV V3<R> getfr(int f) const {
     V3<R> v = fr[0];
 #pragma unroll
@@ -602,14 +608,48 @@ template <class R> ABX_DEV void trk_current(const Tables& T, const View<R>& V, c
   if (k.cell < 0) trk_restart(T, V, P, k);
 }
 
+// The check half of Tracker::get_current (tracker.hpp:235-306): walks the
+// tree and reports what must be re-located, without descending.  Returns
+// 0 when every pad is still valid, 1 when the tree must be rebuilt from the
+// root, 2 when it must be re-descended from universe `ui` in frame `fr` (the
+// tree is already truncated).  The descent itself runs once per iteration of
+// the transport loop for every lane that needs one (descend()).
+template <class R> ABX_DEV int trk_check(const Tables& T, const View<R>& V, Trk<R>& k, int& ui, int& fr) {
+  if (!(k.r.x == k.fr[0].x && k.r.y == k.fr[0].y && k.r.z == k.fr[0].z)) return 1;
+  int first_bad = k.depth;
+#pragma unroll 1
+  for (int i = 0; i < k.depth; i++) {
+    const uint32_t p = k.getpad(i);
+    const int ty = pad_type(p);
+    if (ty == PAD_UNIV) continue;
+    const V3<R> rl = k.getfr(pad_frame(p));
+    if (ty == PAD_CELL) {
+      if (!cell_inside(T, V, pad_idx(p), rl, k.u, k.token)) { first_bad = i; break; }
+    } else {
+      int t[3];
+      get_tile(V.lat[T.univ[pad_idx(p)].lat], rl, k.u, t);
+      if (tile_pack(t) != k.gettile(i)) { first_bad = i; break; }
+    }
+  }
+  if (first_bad == k.depth) return 0;
+  if (first_bad == 0) return 1;
+  const uint32_t back = k.getpad(first_bad - 1);
+  k.depth = first_bad - 1;
+  // universe_id_to_indx[tree.back().id]: a Cell pad is looked up by the
+  // cell's id (cells[].reentry precomputes what that lookup yields).
+  ui = pad_type(back) == PAD_CELL ? T.cells[pad_idx(back)].reentry : pad_idx(back);
+  fr = pad_frame(back);
+  return 2;
+}
+
 // Tracker::get_boundary_condition (tracker.hpp:94-161)
 template <class R> ABX_DEV Bound<R> trk_bc(const Tables& T, const View<R>& V, const ProbT& P, const Trk<R>& k) {
   if (k.cell < 0) return univ_bc(T, V, P.root, k.r, k.u, k.token);
   Bound<R> b{Tol<R>::INF, -1, ABX_BC_VACUUM, 0};
-#pragma unroll
-  for (int i = 0; i < MAXD; i++) {
-    if (i < k.depth) {
-      uint32_t p = k.pad[i];
+#pragma unroll 1
+  for (int i = 0; i < k.depth; i++) {
+    {
+      uint32_t p = k.getpad(i);
       int ty = pad_type(p), id = pad_idx(p);
       V3<R> rl = k.getfr(pad_frame(p));
       if (ty == PAD_CELL) {
@@ -637,15 +677,15 @@ template <class R> ABX_DEV Bound<R> trk_bc(const Tables& T, const View<R>& V, co
 // Tracker::get_nearest_boundary (tracker.hpp:163-225)
 template <class R> ABX_DEV Bound<R> trk_nearest(const Tables& T, const View<R>& V, const ProbT& P, const Trk<R>& k) {
   Bound<R> b = trk_bc(T, V, P, k);
-#pragma unroll
-  for (int i = 0; i < MAXD; i++) {
-    if (i < k.depth) {
-      uint32_t p = k.pad[i];
+#pragma unroll 1
+  for (int i = 0; i < k.depth; i++) {
+    {
+      uint32_t p = k.getpad(i);
       int ty = pad_type(p), id = pad_idx(p);
       V3<R> rl = k.getfr(pad_frame(p));
       if (ty == PAD_LATT) {
         int t[3];
-        tile_unpack(k.tl[i], t);
+        tile_unpack(k.gettile(i), t);
         R d = tile_dist(V.lat[T.univ[id].lat], rl, k.u, t);
         if (d < b.dist && m_abs(d - b.dist) > Tol<R>::BTOL) {
           b.dist = d; b.btype = ABX_BC_NORMAL; b.si = -1; b.token = 0;
@@ -778,10 +818,10 @@ ABX_DEV Bound<R> cells_bc_mixed(const Tables& T, const View<R>& V, int ci, V3<R>
 
 template <class R> ABX_DEV Bound<R> trk_bc_mixed(const Tables& T, const View<R>& V, const ProbT& P, const Trk<R>& k) {
   Bound<R> b{Tol<R>::INF, -1, ABX_BC_VACUUM, 0};
-#pragma unroll
-  for (int i = 0; i < MAXD; i++) {
-    if (i < k.depth) {
-      uint32_t p = k.pad[i];
+#pragma unroll 1
+  for (int i = 0; i < k.depth; i++) {
+    {
+      uint32_t p = k.getpad(i);
       int ty = pad_type(p), id = pad_idx(p);
       V3<R> rl = k.getfr(pad_frame(p));
       if (ty == PAD_CELL) {
@@ -806,15 +846,15 @@ template <class R> ABX_DEV Bound<R> trk_bc_mixed(const Tables& T, const View<R>&
 
 template <class R> ABX_DEV Bound<R> trk_nearest_mixed(const Tables& T, const View<R>& V, const ProbT& P, const Trk<R>& k) {
   Bound<R> b = trk_bc_mixed(T, V, P, k);
-#pragma unroll
-  for (int i = 0; i < MAXD; i++) {
-    if (i < k.depth) {
-      uint32_t p = k.pad[i];
+#pragma unroll 1
+  for (int i = 0; i < k.depth; i++) {
+    {
+      uint32_t p = k.getpad(i);
       int ty = pad_type(p), id = pad_idx(p);
       V3<R> rl = k.getfr(pad_frame(p));
       if (ty == PAD_LATT) {
         int t[3];
-        tile_unpack(k.tl[i], t);
+        tile_unpack(k.gettile(i), t);
         R d = tile_exit(V.lat[T.univ[id].lat], rl, k.u, t);
         if (d < b.dist) { b.dist = d; b.btype = ABX_BC_NORMAL; b.si = -1; b.token = 0; }
       } else if (ty == PAD_CELL) {

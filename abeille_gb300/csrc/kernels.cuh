@@ -402,290 +402,4 @@ ABX_DEV void collide(const TransportArgs<R>& A, const Tables& T, const View<R>& 
   }
 }
 
-template <class R>
-ABX_DEV void do_reflection(const Tables& T, const View<R>& V, const ProbT& P, Trk<R>& k, Lane<R>& L, const Bound<R>& b) {
-  // Tracker::do_reflection (tracker.hpp:314-359); the surface token it sets is
-  // cleared by set_r, and previous-position bookkeeping only feeds cancellation.
-  const SurfT<R> s = V.surf[b.si];
-  V3<R> r_on = add(L.r, scl(L.u, b.dist));
-  if (sizeof(R) == 4) {  // mixed mode: put the point exactly on an axis plane
-    if (s.type == ABX_SURF_XPLANE) r_on.x = s.c[0];
-    else if (s.type == ABX_SURF_YPLANE) r_on.y = s.c[0];
-    else if (s.type == ABX_SURF_ZPLANE) r_on.z = s.c[0];
-  }
-  V3<R> n = surf_norm(s, r_on);
-  R c2 = R(2) * dot(L.u, n);
-  V3<R> nd = sub(L.u, scl(n, c2));
-  // the side token the reference computes before set_r clears it
-  const int32_t side = sizeof(R) == 4 && b.token != 0 ? b.token
-                       : (surf_sign(s, L.r, L.u) < 0 ? -(b.si + 1) : (b.si + 1));
-  L.r = r_on;
-  L.u = dir3(nd.x, nd.y, nd.z);
-  trk_set_r(k, L.r);
-  k.u = L.u;
-  // Mixed mode keeps it: the particle sits on the plane, and with no FP32
-  // distance band the token is what marks that plane as the one it is on.
-  if (sizeof(R) == 4) k.token = side;
-  trk_restart(T, V, P, k);
-}
-
-// Load history h into a lane and locate it (Tracker ctor, DeltaTracker::transport
-// src/delta_tracker.cpp:87-103).
-template <class R>
-ABX_DEV bool lane_load(const TransportArgs<R>& A, const Tables& T, const View<R>& V, Lane<R>& L, Trk<R>& k, uint32_t h) {
-  L.h = h;
-  L.r = mk<R>(A.bank.x[h], A.bank.y[h], A.bank.z[h]);
-  L.u = mk<R>(A.bank.ux[h], A.bank.uy[h], A.bank.uz[h]);
-  L.E = A.bank.E[h];
-  L.w = A.bank.w[h];
-  L.w2 = A.bank.w2 ? A.bank.w2[h] : R(0);
-  L.rng = A.bank.rng[h];
-  L.pid = A.bank.prob ? A.bank.prob[h] : 0;
-  L.rb = L.r;
-  L.dau = 0;
-  L.nsec = 0;
-  L.events = 0;
-  const ProbT& P = T.probs[L.pid];
-  L.g = group_of<R>(V.ebnd + P.eb_off, P.G, L.E);
-  k.r = L.r; k.u = L.u; k.token = 0; k.err = 0;
-  if (L.g >= P.G) {  // energy outside the group structure
-    k.err = ABX_ERR_INVALID;
-    L.mat = -1;
-    return false;
-  }
-  trk_restart(T, V, P, k);
-  if (k.cell < 0) {
-    L.mat = -1;
-    return false;
-  }
-  L.mat = T.cells[k.cell].fill;
-  return true;
-}
-
-template <class R, int TRACK>
-__global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R> A) {
-  const bool TRACE = A.trace != nullptr;
-  const Tables& T = A.T;
-  const View<R> V = make_view<R>(T);
-  DevState* st = A.st;
-  const unsigned lane = threadIdx.x & 31u;
-  const unsigned long long n_hist = st->n_hist;
-  const R kcol = (R)st->kcol;
-  const bool converged = st->converged != 0;
-
-  __shared__ double sh_acc[5];
-  if (threadIdx.x < 5) sh_acc[threadIdx.x] = 0.;
-  __syncthreads();
-
-  Lane<R> L;
-  Trk<R> k;
-  Acc<R> acc;
-  uint32_t ncoll = 0, nflight = 0, nlost = 0;
-  bool active = false, done = false;
-  L.h = 0xffffffffu;
-  L.pid = 0;
-  L.mat = -1;
-  L.nsec = 0;
-  L.dau = 0;
-  L.npos = 0;
-  L.nneg = 0;
-  k.depth = 0;
-
-  while (true) {
-    // ------------------------------------------------ lane refill
-    bool need = !active && !done;
-    unsigned m = __ballot_sync(0xffffffffu, need);
-    if (m) {
-      unsigned leader = __ffs(m) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(&st->next_hist, (unsigned long long)__popc(m));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (need) {
-        unsigned long long h = base + __popc(m & ((1u << lane) - 1u));
-        if (h >= n_hist || st->err) {
-          done = true;
-        } else {
-          active = lane_load(A, T, V, L, k, (uint32_t)h);
-          if (k.err) { raise_err(st, k.err, L.h); done = true; active = false; }
-          else if (!active) {
-            nlost++;
-            A.hist_count[h] = 0;
-          }
-        }
-      }
-    }
-    if (__all_sync(0xffffffffu, done)) break;
-    if (!active) continue;
-
-    // ------------------------------------------------ one flight
-    const ProbT& P = T.probs[L.pid];
-    bool alive = true;
-    bool had_collision = false;
-    L.events++;
-    nflight++;
-    if (TRACK == ABX_TRACK_DELTA) {
-      const R Emaj = V.maj[P.maj_off + L.g];
-      R d_coll = Emaj == R(0) ? Tol<R>::INF : -m_log(R(1) - canon<R>(L.rng)) / Emaj;
-      Bound<R> bound{Tol<R>::INF, -1, ABX_BC_NORMAL, 0};
-      bool crossed = false;
-      trk_move(k, d_coll);
-      trk_current(T, V, P, k);
-      if (k.cell < 0) {
-        trk_set_r(k, L.r);
-        trk_current(T, V, P, k);
-        // Mixed mode: the search is direction-aware at axis planes, so a
-        // particle within the FP32 coincidence band of the wall it leaves
-        // through finds that wall (trk_bc_mixed).
-        bound = sizeof(R) == 8 ? trk_bc(T, V, P, k) : trk_bc_mixed(T, V, P, k);
-        crossed = true;
-      }
-      if (converged && P.has_tle) score_flight(T, V, P, L, d_coll < bound.dist ? d_coll : bound.dist);
-      if (crossed) {
-        if (bound.btype == ABX_BC_VACUUM) {
-          alive = false;
-          acc.hleak += L.w;
-          V3<R> rl = add(L.r, scl(L.u, bound.dist));
-          V3<R> dl = sub(rl, L.rb);
-          acc.hmig += dot(scl(dl, L.w), dl);
-          if (TRACE) trace_rec(A, L, 2, k.cell);
-        } else if (bound.btype == ABX_BC_REFLECTIVE) {
-          do_reflection(T, V, P, k, L, bound);
-          if (k.cell < 0) {
-            if (sizeof(R) == 8) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
-            nlost++;  // mixed mode: counted in `lost` and killed
-            alive = false;
-          }
-          if (TRACE) trace_rec(A, L, 3, k.cell);
-        } else {
-          if (sizeof(R) == 8) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
-          nlost++;
-          alive = false;
-        }
-      } else {
-        L.r = add(L.r, scl(L.u, d_coll));
-        L.mat = T.cells[k.cell].fill;
-        const MatT& M = T.mats[L.mat];
-        const R Et = V.xs[M.xs_off + XS_ET * M.G + L.g];
-        if (Et - Emaj > Tol<R>::MAJ) { raise_err(st, ABX_ERR_MAJORANT, L.h); done = true; active = false; continue; }
-        if (canon<R>(L.rng) < (Et / Emaj)) had_collision = true;
-        if (TRACE) trace_rec(A, L, had_collision ? 1 : 0, k.cell);
-      }
-    } else {
-      const MatT& M = T.mats[L.mat];
-      const R Et = V.xs[M.xs_off + XS_ET * M.G + L.g];
-      R d_coll = Et == R(0) ? Tol<R>::INF : -m_log(R(1) - canon<R>(L.rng)) / Et;
-      Bound<R> bound = sizeof(R) == 8 ? trk_nearest(T, V, P, k) : trk_nearest_mixed(T, V, P, k);
-      R dmin = d_coll < bound.dist ? d_coll : bound.dist;
-      if (converged && P.has_tle) score_flight(T, V, P, L, dmin);
-      acc.htrk += L.w * dmin * V.xs[M.xs_off + XS_VEF * M.G + L.g];
-      if (bound.dist < d_coll || m_abs(bound.dist - d_coll) < Tol<R>::BTOL) {
-        if (bound.btype == ABX_BC_VACUUM) {
-          alive = false;
-          acc.hleak += L.w;
-          V3<R> rl = add(L.r, scl(L.u, bound.dist));
-          V3<R> dl = sub(rl, L.rb);
-          acc.hmig += dot(scl(dl, L.w), dl);
-          if (TRACE) trace_rec(A, L, 2, k.cell);
-        } else if (bound.btype == ABX_BC_REFLECTIVE) {
-          do_reflection(T, V, P, k, L, bound);
-          if (k.cell < 0) {
-            if (sizeof(R) == 8) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
-            nlost++;  // mixed mode: counted in `lost` and killed
-            alive = false;
-          }
-          if (TRACE) trace_rec(A, L, 3, k.cell);
-        } else {
-          const int prev = k.cell;
-          trk_move(k, bound.dist);
-          k.token = -bound.token;
-          trk_current(T, V, P, k);
-          L.r = add(L.r, scl(L.u, bound.dist));
-          if (sizeof(R) == 4 && (k.cell < 0 || (k.cell == prev && bound.dist == R(0)))) {
-            // mixed mode: step off a surface crossing FP32 cannot resolve
-            L.r = add(L.r, scl(L.u, R(4) * Tol<R>::SC));
-            trk_set_r(k, L.r);
-            trk_restart(T, V, P, k);
-          }
-          if (k.cell < 0) {
-            if (sizeof(R) == 8) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
-            nlost++;
-            alive = false;
-          } else {
-            L.mat = T.cells[k.cell].fill;
-          }
-          if (TRACE) trace_rec(A, L, 5, k.cell);
-        }
-      } else {
-        L.r = add(L.r, scl(L.u, d_coll));
-        trk_move(k, d_coll);
-        had_collision = true;
-        if (TRACE) trace_rec(A, L, 1, k.cell);
-      }
-    }
-    if (k.err) { raise_err(st, k.err, L.h); done = true; active = false; continue; }
-    if (alive && had_collision) {
-      ncoll++;
-      collide(A, T, V, P, L, acc, converged, kcol, alive);
-      k.u = L.u;
-      if (TRACE) trace_rec(A, L, 4, k.cell);
-    }
-    if (!alive) {
-      if (L.nsec > 0) {
-        // Particle::resurect (include/simulation/particle.hpp:170-182)
-        L.nsec--;
-        uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
-        const R* sp = A.sec + ((uint64_t)gt * A.sec_cap + L.nsec) * 9;
-        L.r = mk<R>(sp[0], sp[1], sp[2]);
-        L.u = mk<R>(sp[3], sp[4], sp[5]);
-        L.E = sp[6]; L.w = sp[7]; L.w2 = sp[8];
-        L.g = group_of<R>(V.ebnd + P.eb_off, P.G, L.E);
-        if (L.g >= P.G) { raise_err(st, ABX_ERR_INVALID, L.h); done = true; active = false; continue; }
-        trk_set_r(k, L.r);
-        k.u = L.u;
-        trk_restart(T, V, P, k);
-        if (k.cell < 0 || k.err) { raise_err(st, ABX_ERR_LOST_PARTICLE, L.h); done = true; active = false; continue; }
-        L.mat = T.cells[k.cell].fill;
-        if (TRACE) trace_rec(A, L, 6, k.cell);
-      } else {
-        A.hist_count[L.h] = L.dau;
-        acc.flush(sh_acc);
-        active = false;
-      }
-    } else if (sizeof(R) == 4 && L.events > 100000u) {
-      // mixed mode: a history this long is a geometry rounding trap, not
-      // physics; it is counted in `lost` and ended
-      nlost++;
-      A.hist_count[L.h] = L.dau;
-      acc.flush(sh_acc);
-      active = false;
-    } else if (L.events > A.max_events) {
-      raise_err(st, ABX_ERR_TIMEOUT, L.h);
-      done = true;
-      active = false;
-    }
-  }
-  acc.flush(sh_acc);
-  unsigned long long c[5] = {ncoll, nflight, nlost, (unsigned long long)L.npos, (unsigned long long)L.nneg};
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-    for (int i = 0; i < 5; i++) c[i] += __shfl_down_sync(0xffffffffu, c[i], o);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    atomicAdd(&st->scores[0], sh_acc[0]);
-    atomicAdd(&st->scores[1], sh_acc[1]);
-    atomicAdd(&st->scores[2], sh_acc[2]);
-    atomicAdd(&st->scores[4], sh_acc[3]);
-    atomicAdd(&st->scores[5], sh_acc[4]);
-  }
-  if (lane == 0) {
-    atomicAdd(&st->collisions, c[0]);
-    atomicAdd(&st->flights, c[1]);
-    atomicAdd(&st->lost, c[2]);
-    atomicAdd(&st->site_pos, c[3]);
-    atomicAdd(&st->site_neg, c[4]);
-  }
-}
-
 }  // namespace abx

@@ -1,7 +1,7 @@
 // FP64 parity translation unit: every kernel here runs in double, in the
 // reference's operation order, compiled with --fmad=false so no
 // multiply-add is contracted.
-#include "kernels.cuh"
+#include "transport_loop.cuh"
 #include "launch.h"
 
 namespace abx {

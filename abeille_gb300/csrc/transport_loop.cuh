@@ -1,0 +1,418 @@
+// The transport loop: one persistent launch, one lane per history, written as
+// a per-lane event state machine.
+//
+// Every lane keeps its history's state in registers and sits in one phase.
+// Each pass of the loop visits the phases in a fixed order, and the lanes in
+// a phase execute it together: refill (take the next history), flight
+// (sample a distance, move, check the geometry tree), descend (re-locate in
+// the CSG tree: the only copy of the descent code), start / reflect / cross /
+// resurrect checks, moved (real-or-virtual test), boundary (leak or reflect),
+// collide, dead.  A lane runs through as many phases per pass as its history
+// allows (a tile crossing followed by a real collision is one pass).  Each
+// history still performs exactly the reference's sequence of operations and
+// draws; only the interleaving across lanes changes.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace abx {
+
+enum : int {
+  PH_REFILL = 0,
+  PH_WAIT,     // waiting for the descend phase; continues in `after`
+  PH_START,
+  PH_FLIGHT,
+  PH_MOVED,
+  PH_LOST,
+  PH_REFL,
+  PH_CROSSED,
+  PH_COLL,
+  PH_DEAD,
+  PH_RES,
+  PH_DONE
+};
+
+// Load history h into a lane (DeltaTracker::transport, src/delta_tracker.cpp:87-103);
+// its location is found by the next descend phase.
+template <class R>
+ABX_DEV bool lane_load(const TransportArgs<R>& A, const Tables& T, const View<R>& V, Lane<R>& L, Trk<R>& k,
+                       uint32_t h) {
+  L.h = h;
+  L.r = mk<R>(A.bank.x[h], A.bank.y[h], A.bank.z[h]);
+  L.u = mk<R>(A.bank.ux[h], A.bank.uy[h], A.bank.uz[h]);
+  L.E = A.bank.E[h];
+  L.w = A.bank.w[h];
+  L.w2 = A.bank.w2 ? A.bank.w2[h] : R(0);
+  L.rng = A.bank.rng[h];
+  L.pid = A.bank.prob ? A.bank.prob[h] : 0;
+  L.rb = L.r;
+  L.dau = 0;
+  L.nsec = 0;
+  L.events = 0;
+  const ProbT& P = T.probs[L.pid];
+  L.g = group_of<R>(V.ebnd + P.eb_off, P.G, L.E);
+  k.r = L.r;
+  k.u = L.u;
+  k.token = 0;
+  k.err = 0;
+  k.depth = 0;
+  if (L.g >= P.G) {  // energy outside the group structure
+    k.err = ABX_ERR_INVALID;
+    return false;
+  }
+  return true;
+}
+
+// Tracker::do_reflection (tracker.hpp:314-359) without the re-location, which
+// the descend phase performs.  The surface token it sets is cleared by set_r
+// in the reference; the mixed mode keeps it (the particle sits on the plane
+// and, with no FP32 distance band, the token marks it as the one it is on).
+// Previous-position bookkeeping only feeds cancellation and is not carried.
+template <class R>
+ABX_DEV void reflect_move(const View<R>& V, Trk<R>& k, Lane<R>& L, const Bound<R>& b) {
+  const SurfT<R> s = V.surf[b.si];
+  V3<R> r_on = add(L.r, scl(L.u, b.dist));
+  if (sizeof(R) == 4) {  // mixed mode: put the point exactly on an axis plane
+    if (s.type == ABX_SURF_XPLANE) r_on.x = s.c[0];
+    else if (s.type == ABX_SURF_YPLANE) r_on.y = s.c[0];
+    else if (s.type == ABX_SURF_ZPLANE) r_on.z = s.c[0];
+  }
+  V3<R> n = surf_norm(s, r_on);
+  R c2 = R(2) * dot(L.u, n);
+  V3<R> nd = sub(L.u, scl(n, c2));
+  const int32_t side = sizeof(R) == 4 && b.token != 0 ? b.token
+                       : (surf_sign(s, L.r, L.u) < 0 ? -(b.si + 1) : (b.si + 1));
+  L.r = r_on;
+  L.u = dir3(nd.x, nd.y, nd.z);
+  trk_set_r(k, L.r);
+  k.u = L.u;
+  if (sizeof(R) == 4) k.token = side;
+}
+
+template <class R, int TRACK>
+__global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R> A) {
+  const bool TRACE = A.trace != nullptr;
+  const Tables& T = A.T;
+  const View<R> V = make_view<R>(T);
+  DevState* st = A.st;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned long long n_hist = st->n_hist;
+  const R kcol = (R)st->kcol;
+  const bool converged = st->converged != 0;
+  const uint32_t ev_limit = sizeof(R) == 4 ? 100000u : (uint32_t)(A.max_events < 0xffffffffull ? A.max_events : 0xffffffffull);
+
+  __shared__ double sh_acc[5];
+  if (threadIdx.x < 5) sh_acc[threadIdx.x] = 0.;
+  __syncthreads();
+
+  Lane<R> L;
+  Trk<R> k;
+  Acc<R> acc;
+  uint32_t ncoll = 0, nflight = 0, nlost = 0;
+  int ph = PH_REFILL, after = PH_REFILL, dmode = 0, dui = 0, dfr = 0, prev_cell = -1;
+  R dcol = R(0);
+  bool done = false;
+  L.h = 0xffffffffu;
+  L.pid = 0;
+  L.mat = -1;
+  L.nsec = 0;
+  L.dau = 0;
+  L.npos = 0;
+  L.nneg = 0;
+  L.events = 0;
+  L.g = 0;
+  k.depth = 0;
+  k.cell = -1;
+  k.err = 0;
+
+#define ABX_FAIL(code)            \
+  {                               \
+    raise_err(st, (code), L.h);   \
+    done = true;                  \
+    ph = PH_DONE;                 \
+  }
+
+  while (true) {
+    // ---------------------------------------------------------------- refill
+    const bool need = ph == PH_REFILL && !done;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const unsigned leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(&st->next_hist, (unsigned long long)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const unsigned long long h = base + __popc(m & ((1u << lane) - 1u));
+        if (h >= n_hist || st->err) {
+          done = true;
+          ph = PH_DONE;
+        } else if (!lane_load(A, T, V, L, k, (uint32_t)h)) {
+          ABX_FAIL(k.err);
+        } else {
+          dmode = 1;
+          after = PH_START;
+          ph = PH_WAIT;
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, done)) break;
+
+    // ---------------------------------------------------------------- flight
+    if (ph == PH_FLIGHT) {
+      const ProbT& P = T.probs[L.pid];
+      L.events++;
+      nflight++;
+      if (TRACK == ABX_TRACK_DELTA) {
+        // DeltaTracker::transport (src/delta_tracker.cpp:105-118)
+        const R Emaj = V.maj[P.maj_off + L.g];
+        dcol = Emaj == R(0) ? Tol<R>::INF : -m_log(R(1) - canon<R>(L.rng)) / Emaj;
+        trk_move(k, dcol);
+        const int r = trk_check(T, V, k, dui, dfr);
+        if (r) {
+          dmode = r;
+          after = PH_MOVED;
+          ph = PH_WAIT;
+        } else {
+          ph = PH_MOVED;
+        }
+      } else {
+        // SurfaceTracker::transport (src/surface_tracker.cpp:72-150)
+        const MatT& M = T.mats[L.mat];
+        const R Et = V.xs[M.xs_off + XS_ET * M.G + L.g];
+        dcol = Et == R(0) ? Tol<R>::INF : -m_log(R(1) - canon<R>(L.rng)) / Et;
+        const Bound<R> b = sizeof(R) == 8 ? trk_nearest(T, V, P, k) : trk_nearest_mixed(T, V, P, k);
+        const R dmin = dcol < b.dist ? dcol : b.dist;
+        if (converged && P.has_tle) score_flight(T, V, P, L, dmin);
+        acc.htrk += L.w * dmin * V.xs[M.xs_off + XS_VEF * M.G + L.g];
+        if (b.dist < dcol || m_abs(b.dist - dcol) < Tol<R>::BTOL) {
+          if (b.btype == ABX_BC_VACUUM) {
+            acc.hleak += L.w;
+            const V3<R> dl = sub(add(L.r, scl(L.u, b.dist)), L.rb);
+            acc.hmig += dot(scl(dl, L.w), dl);
+            if (TRACE) trace_rec(A, L, 2, k.cell);
+            ph = PH_DEAD;
+          } else if (b.btype == ABX_BC_REFLECTIVE) {
+            reflect_move(V, k, L, b);
+            dmode = 1;
+            after = PH_REFL;
+            ph = PH_WAIT;
+          } else {
+            // Tracker::cross_surface + get_current (tracker.hpp:227-231)
+            prev_cell = k.cell;
+            trk_move(k, b.dist);
+            k.token = -b.token;
+            L.r = add(L.r, scl(L.u, b.dist));
+            dcol = b.dist;
+            const int r = trk_check(T, V, k, dui, dfr);
+            if (r) {
+              dmode = r;
+              after = PH_CROSSED;
+              ph = PH_WAIT;
+            } else {
+              ph = PH_CROSSED;
+            }
+          }
+        } else {
+          L.r = add(L.r, scl(L.u, dcol));
+          trk_move(k, dcol);
+          if (TRACE) trace_rec(A, L, 1, k.cell);
+          ph = PH_COLL;
+        }
+      }
+    }
+
+    // --------------------------------------------------------------- descend
+    if (ph == PH_WAIT) {
+      // CellUniverse/RectLattice::get_cell: re-descent from the first invalid
+      // pad, or from the root (restart_get_current) when that fails or when the
+      // tree must be rebuilt.
+      const ProbT& P = T.probs[L.pid];
+      int cell = -1;
+      if (dmode == 2) {
+        cell = univ_get_cell(T, V, k, dui, dfr, k.getfr(dfr));
+        if (cell < 0) dmode = 1;
+      }
+      if (dmode == 1) {
+        k.depth = 0;
+        cell = univ_get_cell(T, V, k, P.root, 0, k.r);
+      }
+      k.cell = cell;
+      dmode = 0;
+      ph = after;
+      if (k.err) ABX_FAIL(k.err);
+    }
+
+    // ------------------------------------------------ post-descend checks
+    if (ph == PH_START) {
+      if (k.cell < 0) {  // lost at birth: a warning in the reference, the particle is killed
+        nlost++;
+        A.hist_count[L.h] = 0;
+        ph = PH_REFILL;
+      } else {
+        L.mat = T.cells[k.cell].fill;
+        ph = PH_FLIGHT;
+      }
+    } else if (ph == PH_RES) {
+      if (k.cell < 0) ABX_FAIL(ABX_ERR_LOST_PARTICLE) else {
+        L.mat = T.cells[k.cell].fill;
+        if (TRACE) trace_rec(A, L, 6, k.cell);
+        ph = PH_FLIGHT;
+      }
+    } else if (ph == PH_REFL) {
+      if (k.cell < 0) {
+        if (sizeof(R) == 8) ABX_FAIL(ABX_ERR_LOST_PARTICLE) else {
+          nlost++;  // mixed mode: counted in `lost` and killed
+          ph = PH_DEAD;
+        }
+      } else {
+        if (TRACE) trace_rec(A, L, 3, k.cell);
+        ph = PH_FLIGHT;
+      }
+    } else if (ph == PH_CROSSED) {
+      if (sizeof(R) == 4 && prev_cell != -2 && (k.cell < 0 || (k.cell == prev_cell && dcol == R(0)))) {
+        // mixed mode: step off a surface crossing FP32 cannot resolve
+        L.r = add(L.r, scl(L.u, R(4) * Tol<R>::SC));
+        trk_set_r(k, L.r);
+        prev_cell = -2;
+        dmode = 1;
+        after = PH_CROSSED;
+        ph = PH_WAIT;
+      } else if (k.cell < 0) {
+        if (sizeof(R) == 8) ABX_FAIL(ABX_ERR_LOST_PARTICLE) else {
+          nlost++;
+          ph = PH_DEAD;
+        }
+      } else {
+        L.mat = T.cells[k.cell].fill;
+        if (TRACE) trace_rec(A, L, 5, k.cell);
+        ph = PH_FLIGHT;
+      }
+    }
+
+    // ----------------------------------------------------------------- moved
+    if (ph == PH_MOVED) {
+      if (k.cell < 0) {
+        // flew out of the geometry: back to the last position, find the
+        // boundary condition (src/delta_tracker.cpp:120-127)
+        trk_set_r(k, L.r);
+        dmode = 1;
+        after = PH_LOST;
+        ph = PH_WAIT;
+      } else {
+        const ProbT& P = T.probs[L.pid];
+        if (converged && P.has_tle) score_flight(T, V, P, L, dcol);
+        L.r = add(L.r, scl(L.u, dcol));
+        L.mat = T.cells[k.cell].fill;
+        const MatT& M = T.mats[L.mat];
+        const R Et = V.xs[M.xs_off + XS_ET * M.G + L.g];
+        const R Emaj = V.maj[P.maj_off + L.g];
+        if (Et - Emaj > Tol<R>::MAJ) ABX_FAIL(ABX_ERR_MAJORANT) else {
+          const bool real = canon<R>(L.rng) < (Et / Emaj);
+          if (TRACE) trace_rec(A, L, real ? 1 : 0, k.cell);
+          ph = real ? PH_COLL : PH_FLIGHT;
+        }
+      }
+    }
+
+    // -------------------------------------------------------------- boundary
+    if (ph == PH_LOST) {
+      const ProbT& P = T.probs[L.pid];
+      const Bound<R> b = sizeof(R) == 8 ? trk_bc(T, V, P, k) : trk_bc_mixed(T, V, P, k);
+      if (converged && P.has_tle) score_flight(T, V, P, L, dcol < b.dist ? dcol : b.dist);
+      if (b.btype == ABX_BC_VACUUM) {
+        acc.hleak += L.w;
+        const V3<R> dl = sub(add(L.r, scl(L.u, b.dist)), L.rb);
+        acc.hmig += dot(scl(dl, L.w), dl);
+        if (TRACE) trace_rec(A, L, 2, k.cell);
+        ph = PH_DEAD;
+      } else if (b.btype == ABX_BC_REFLECTIVE) {
+        reflect_move(V, k, L, b);
+        dmode = 1;
+        after = PH_REFL;
+        ph = PH_WAIT;
+      } else if (sizeof(R) == 8) {
+        ABX_FAIL(ABX_ERR_LOST_PARTICLE);
+      } else {
+        nlost++;
+        ph = PH_DEAD;
+      }
+    }
+
+    // --------------------------------------------------------------- collide
+    if (ph == PH_COLL) {
+      const ProbT& P = T.probs[L.pid];
+      bool alive = true;
+      ncoll++;
+      collide(A, T, V, P, L, acc, converged, kcol, alive);
+      k.u = L.u;
+      if (TRACE) trace_rec(A, L, 4, k.cell);
+      ph = alive ? PH_FLIGHT : PH_DEAD;
+    }
+
+    // ------------------------------------------------------------------ dead
+    if (ph == PH_DEAD) {
+      if (L.nsec > 0) {
+        // Particle::resurect (include/simulation/particle.hpp:170-182)
+        const ProbT& P = T.probs[L.pid];
+        L.nsec--;
+        const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+        const R* sp = A.sec + ((uint64_t)gt * A.sec_cap + L.nsec) * 9;
+        L.r = mk<R>(sp[0], sp[1], sp[2]);
+        L.u = mk<R>(sp[3], sp[4], sp[5]);
+        L.E = sp[6];
+        L.w = sp[7];
+        L.w2 = sp[8];
+        L.g = group_of<R>(V.ebnd + P.eb_off, P.G, L.E);
+        if (L.g >= P.G) ABX_FAIL(ABX_ERR_INVALID) else {
+          trk_set_r(k, L.r);
+          k.u = L.u;
+          dmode = 1;
+          after = PH_RES;
+          ph = PH_WAIT;
+        }
+      } else {
+        A.hist_count[L.h] = L.dau;
+        acc.flush(sh_acc);
+        ph = PH_REFILL;
+      }
+    }
+
+    if (ph != PH_REFILL && ph != PH_DONE && L.events > ev_limit) {
+      if (sizeof(R) == 4) {
+        // mixed mode: a history this long is a geometry rounding trap, not
+        // physics; it is counted in `lost` and ended
+        nlost++;
+        A.hist_count[L.h] = L.dau;
+        acc.flush(sh_acc);
+        ph = PH_REFILL;
+      } else {
+        ABX_FAIL(ABX_ERR_TIMEOUT);
+      }
+    }
+  }
+#undef ABX_FAIL
+  acc.flush(sh_acc);
+  unsigned long long c[5] = {ncoll, nflight, nlost, (unsigned long long)L.npos, (unsigned long long)L.nneg};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int i = 0; i < 5; i++) c[i] += __shfl_down_sync(0xffffffffu, c[i], o);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(&st->scores[0], sh_acc[0]);
+    atomicAdd(&st->scores[1], sh_acc[1]);
+    atomicAdd(&st->scores[2], sh_acc[2]);
+    atomicAdd(&st->scores[4], sh_acc[3]);
+    atomicAdd(&st->scores[5], sh_acc[4]);
+  }
+  if (lane == 0) {
+    atomicAdd(&st->collisions, c[0]);
+    atomicAdd(&st->flights, c[1]);
+    atomicAdd(&st->lost, c[2]);
+    atomicAdd(&st->site_pos, c[3]);
+    atomicAdd(&st->site_neg, c[4]);
+  }
+}
+
+}  // namespace abx

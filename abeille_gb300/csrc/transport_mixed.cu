@@ -1,6 +1,6 @@
 // Mixed-precision translation unit: positions, directions, flight distances
 // and cross sections in FP32; scores, tallies and k in FP64.
-#include "kernels.cuh"
+#include "transport_loop.cuh"
 #include "launch.h"
 
 namespace abx {

@@ -144,21 +144,36 @@ def test_reference_known_answers_on_gpu(name, precision):
 
 
 def test_mixed_precision_statistics_config0():
-    """FP32 tracking / FP64 tallies: k within 2 sigma of the FP64 path and at
-    least 95 % of flux bins with |z| < 2."""
+    """FP32 tracking / FP64 tallies against the FP64 path: k within 2 sigma and
+    flux bins with |z| < 2.
+
+    The standard deviations come from independent replicas (different seeds):
+    generation-to-generation statistics of one power iteration underestimate
+    the error because successive generations are correlated (two FP64 runs
+    with different seeds already put only ~89 % of config-0 bins inside
+    |z| < 2 with those).  With 24 replicas per precision the expected fraction
+    under agreement is ~0.95 with a binomial spread of ~0.013 over 289 bins,
+    so the bar is 0.92."""
+    R = 24
     res = {}
     for prec in ("fp64", "mixed"):
-        eng = Engine(decks.config0(nparticles=20000).build(precision=prec), 0)
-        st, _, _ = eng.run_power_iteration(40, 10)
-        t = eng.tally(0)
-        g = t["generations"]
-        res[prec] = (st, t["avg"], np.sqrt(t["var"] / g))
-    (s64, a64, e64), (s32, a32, e32) = res["fp64"], res["mixed"]
-    dk = abs(s32["kcol_avg"] - s64["kcol_avg"])
-    assert dk < 2 * np.hypot(s32["kcol_std"], s64["kcol_std"]) + 1e-5, (s32["kcol_avg"], s64["kcol_avg"])
-    m = (e64 > 0) & (e32 > 0)
-    z = (a32[m] - a64[m]) / np.hypot(e32[m], e64[m])
-    assert np.mean(np.abs(z) < 2) >= 0.95
+        ks, avgs = [], []
+        for rep in range(R):
+            b = decks.config0(nparticles=5000)
+            b.seed = 1000 + rep
+            eng = Engine(b.build(precision=prec), 0)
+            st, _, _ = eng.run_power_iteration(40, 10)
+            ks.append(st["kcol_avg"])
+            avgs.append(eng.tally(0)["avg"])
+            eng.close()
+        res[prec] = (np.array(ks), np.array(avgs))
+    (k64, a64), (k32, a32) = res["fp64"], res["mixed"]
+    dk = (k32.mean() - k64.mean()) / np.sqrt(k32.var(ddof=1) / R + k64.var(ddof=1) / R)
+    assert abs(dk) < 2, (k32.mean(), k64.mean(), dk)
+    z = (a32.mean(0) - a64.mean(0)) / np.sqrt(a32.var(0, ddof=1) / R + a64.var(0, ddof=1) / R)
+    frac = np.mean(np.abs(z) < 2)
+    print(f"mixed vs fp64: dk = {dk:.2f} sigma, {frac:.3f} of {z.size} bins with |z| < 2")
+    assert frac >= 0.92
 
 
 def test_errors_leave_the_context_usable():
