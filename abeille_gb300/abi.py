@@ -148,6 +148,8 @@ PROTOTYPES = {
     "abx_sample_sources": (C.c_int, [C.c_void_p, C.c_uint64, C.c_size_t, C.POINTER(Particle)]),
     "abx_transport": (C.c_int, [C.c_void_p, C.POINTER(Particle), C.c_size_t, C.c_double, C.c_int,
                                 C.POINTER(Site), C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(Scores)]),
+    "abx_transport_noalloc": (C.c_int, [C.c_void_p, C.POINTER(Particle), C.c_size_t, C.c_double, C.c_int,
+                                        C.POINTER(Site), C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(Scores)]),
     "abx_tally_record_generation": (C.c_int, [C.c_void_p, C.c_double]),
     "abx_tally_clear_generation": (C.c_int, [C.c_void_p]),
     "abx_tally_read": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,

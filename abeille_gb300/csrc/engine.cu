@@ -12,6 +12,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1215,6 +1216,136 @@ extern "C" int abx_transport(abx_ctx* c, const abx_particle* bank, size_t n, dou
     CUDA_TRY(cudaMemcpyAsync(sites, c->aos_out, ns * sizeof(abx_site), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
   }
+  return ABX_OK;
+}
+
+// ------------------------------------------------- transport, no allocation
+// abx_transport_noalloc: the transport step for callers that must not
+// allocate device memory while they run -- hosts that route every device
+// allocation through their own pool and forbid direct cudaMalloc, loops that
+// cannot afford the device synchronisation cudaMalloc/cudaFree imply, and
+// processes running at their memory budget, where a late allocation can
+// fail.  The caller owns the bank and
+// site buffers (device memory); every per-call scratch array -- the SoA bank
+// and fission-site arrays, per-history site counts, their prefix sums --
+// lives in one file-scope device array of fixed size, reserved when the
+// library is loaded on a device and held until the process exits.
+static constexpr size_t NA_HIST = 16384;          // histories per call
+static constexpr size_t NA_SITES = 4 * NA_HIST;   // fission sites per call
+static constexpr size_t na_round(size_t b) { return (b + 255) / 256 * 256; }
+static constexpr size_t NA_BANK_ARRAY = na_round(NA_HIST * 8);   // one SoA bank column (8-byte worst case)
+static constexpr size_t NA_SITE_ARRAY = na_round(NA_SITES * 8);  // one SoA site column
+static constexpr size_t NA_BLOCKS = (NA_HIST + SCAN_CHUNK - 1) / SCAN_CHUNK + 1;
+static constexpr size_t NA_BYTES = 12 * NA_BANK_ARRAY + 8 * NA_SITE_ARRAY + 2 * na_round(NA_SITES * 4) +
+                                   2 * na_round(NA_HIST * 4) + na_round(NA_BLOCKS * 4);
+static __device__ __align__(256) unsigned char g_transport_scratch[NA_BYTES];
+
+// The array's device address, looked up once per device with that device
+// current (host code cannot use the symbol itself as a device pointer).
+static std::mutex g_scratch_mu;
+static void* g_scratch_addr[256];
+static int scratch_address(int device, unsigned char** out) {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (device < 0 || device >= 256) return fail(ABX_ERR_INVALID, "device %d out of range", device);
+  if (!g_scratch_addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_transport_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(ABX_ERR_CUDA, "cudaGetSymbolAddress(transport scratch) failed: %s", cudaGetErrorString(e));
+    g_scratch_addr[device] = p;
+  }
+  *out = (unsigned char*)g_scratch_addr[device];
+  return ABX_OK;
+}
+
+template <class R> static void na_carve(unsigned char* base, BankT<R>& b, SiteT<R>& s, uint32_t*& counts,
+                                        uint32_t*& offsets, uint32_t*& blocks) {
+  unsigned char* p = base;
+  R** br[] = {&b.x, &b.y, &b.z, &b.ux, &b.uy, &b.uz, &b.E, &b.w, &b.w2};
+  for (R** a : br) { *a = (R*)p; p += NA_BANK_ARRAY; }
+  uint64_t** bu[] = {&b.rng, &b.hid, &b.fam};
+  for (uint64_t** a : bu) { *a = (uint64_t*)p; p += NA_BANK_ARRAY; }
+  b.prob = nullptr;
+  R** sr[] = {&s.x, &s.y, &s.z, &s.ux, &s.uy, &s.uz, &s.E, &s.w};
+  for (R** a : sr) { *a = (R*)p; p += NA_SITE_ARRAY; }
+  s.hist = (uint32_t*)p; p += na_round(NA_SITES * 4);
+  s.dau = (uint32_t*)p; p += na_round(NA_SITES * 4);
+  counts = (uint32_t*)p; p += na_round(NA_HIST * 4);
+  offsets = (uint32_t*)p; p += na_round(NA_HIST * 4);
+  blocks = (uint32_t*)p;
+}
+
+template <class R>
+static int transport_noalloc_impl(abx_ctx* c, unsigned char* scratch, const abx_particle* bank_dev, size_t n,
+                                  size_t site_cap, abx_site* sites_dev) {
+  BankT<R> b;
+  SiteT<R> s;
+  uint32_t *counts, *offsets, *blocks;
+  na_carve<R>(scratch, b, s, counts, offsets, blocks);
+  k_bank_from_aos<R><<<grid_for(n), 256, 0, c->stream>>>(bank_dev, n, b);
+  TransportArgs<R> A{};
+  A.T = c->D.T;
+  A.T.tally_gen = c->tally_gen;
+  A.bank = b;
+  A.sites = s;
+  A.site_cap = c->prob0.mode == ABX_MODE_K_EIGENVALUE ? std::min(site_cap, NA_SITES) : 0;
+  A.hist_count = counts;
+  A.sec = nullptr;
+  A.sec_cap = 0;
+  A.st = c->st;
+  A.trace = nullptr;
+  A.max_events = c->max_events;
+  if constexpr (sizeof(R) == 4) launch_transport_f(A, c->prob0.tracking, false, c->grid, c->block, c->stream);
+  else launch_transport_d(A, c->prob0.tracking, false, c->grid, c->block, c->stream);
+  CUDA_TRY(cudaGetLastError());
+  unsigned nb = (unsigned)((n + SCAN_CHUNK - 1) / SCAN_CHUNK);
+  if (nb == 0) nb = 1;
+  k_scan_reduce<<<nb, SCAN_T, 0, c->stream>>>(counts, c->st, blocks);
+  k_scan_blocks<<<1, 1024, 0, c->stream>>>(blocks, (int)nb);
+  k_scan_apply<<<nb, SCAN_T, 0, c->stream>>>(counts, c->st, blocks, offsets);
+  if (sites_dev && A.site_cap)
+    k_sites_to_aos<R><<<grid_for(A.site_cap), 256, 0, c->stream>>>(s, c->st, offsets, b, sites_dev, A.site_cap);
+  CUDA_TRY(cudaGetLastError());
+  return ABX_OK;
+}
+
+extern "C" int abx_transport_noalloc(abx_ctx* c, const abx_particle* bank_dev, size_t n, double kcol, int converged,
+                                     abx_site* sites_dev, size_t site_capacity, size_t* n_sites, abx_scores* scores) {
+  if (!c || (!bank_dev && n)) return fail(ABX_ERR_INVALID, "bad arguments");
+  if (!(kcol > 0)) return fail(ABX_ERR_INVALID, "kcol must be positive");
+  if (n > NA_HIST)
+    return fail(ABX_ERR_CAPACITY, "abx_transport_noalloc takes at most %zu histories per call (got %zu)", NA_HIST, n);
+  if (site_capacity > NA_SITES)
+    return fail(ABX_ERR_CAPACITY, "abx_transport_noalloc holds at most %zu fission sites per call (asked for %zu)",
+                NA_SITES, site_capacity);
+  if (c->prob0.mode == ABX_MODE_FIXED_SOURCE && c->fissile_any)
+    return fail(ABX_ERR_UNSUPPORTED, "fixed-source fission secondaries need abx_transport");
+  if (cudaSetDevice(c->device) != cudaSuccess) return fail(ABX_ERR_CUDA, "cudaSetDevice failed");
+  unsigned char* scratch = nullptr;
+  int rc = scratch_address(c->device, &scratch);
+  if (rc) return rc;
+  const bool keig = c->prob0.mode == ABX_MODE_K_EIGENVALUE;
+  k_step_begin<<<1, 1, 0, c->stream>>>(c->st, n, kcol, converged, 0);
+  rc = mixed_of(c) ? transport_noalloc_impl<float>(c, scratch, bank_dev, n, site_capacity, sites_dev)
+                   : transport_noalloc_impl<double>(c, scratch, bank_dev, n, site_capacity, sites_dev);
+  if (rc) return rc;
+  if ((rc = check_state(c)) != ABX_OK) return rc;
+  const DevState& h = *c->st_host;
+  size_t ns = keig ? (size_t)h.site_count : 0;
+  if (n_sites) *n_sites = ns;
+  if (scores) {
+    scores->k_col = h.scores[0];
+    scores->k_abs = h.scores[1];
+    scores->k_trk = h.scores[2];
+    scores->k_tot = h.scores[3];
+    scores->leakage = h.scores[4];
+    scores->mig_area = h.scores[5];
+    scores->collisions = h.collisions;
+    scores->flights = h.flights;
+    scores->lost = h.lost;
+  }
+  if (keig && ns > site_capacity)
+    return fail(ABX_ERR_CAPACITY, "fission bank capacity %zu < %zu sites", site_capacity, ns);
   return ABX_OK;
 }
 

@@ -304,6 +304,26 @@ int abx_transport(abx_ctx* ctx, const abx_particle* bank, size_t n, double kcol,
                   int converged, abx_site* sites, size_t site_capacity,
                   size_t* n_sites, abx_scores* scores);
 
+/* abx_transport without device allocation.  No counterpart in the reference.
+ * For callers that cannot allocate device memory while they run: hosts whose
+ * every device allocation goes through their own memory pool, loops that
+ * cannot afford the device synchronisation cudaMalloc/cudaFree imply, and
+ * processes at their memory budget, where a late allocation can fail.
+ * `bank_dev` and `sites_dev` are device buffers the caller owns (layouts as
+ * abx_particle / abx_site); *n_sites and *scores come back on the host.
+ * Limits: at most 16384 histories and 65536 fission sites per call (larger
+ * requests return ABX_ERR_CAPACITY); fixed-source problems with fissile
+ * materials are refused (their secondaries need abx_transport).
+ * All per-call scratch is one fixed 6 MB device array, reserved on every GPU
+ * that loads the library and held until the process exits.  Every call uses
+ * that same array, so calls that overlap on the GPU race.  The first call on
+ * a device looks the array's address up; make that call before any stream
+ * capture. */
+int abx_transport_noalloc(abx_ctx* ctx, const abx_particle* bank_dev, size_t n,
+                          double kcol, int converged, abx_site* sites_dev,
+                          size_t site_capacity, size_t* n_sites,
+                          abx_scores* scores);
+
 /* MeshTally::record_generation / clear_generation (src/mesh_tally.cpp:121-152). */
 int abx_tally_record_generation(abx_ctx* ctx, double multiplier);
 int abx_tally_clear_generation(abx_ctx* ctx);
