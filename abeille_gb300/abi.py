@@ -164,6 +164,7 @@ PROTOTYPES = {
     "abx_set_trace": (C.c_int, [C.c_void_p, C.c_uint32, C.c_size_t]),
     "abx_get_trace": (C.c_int, [C.c_void_p, C.POINTER(TraceRec), C.c_size_t, C.POINTER(C.c_size_t)]),
     "abx_last_transport_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "abx_set_l2_flush": (C.c_int, [C.c_void_p, C.c_size_t]),
 }
 
 _lib = None

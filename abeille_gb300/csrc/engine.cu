@@ -637,6 +637,8 @@ struct abx_context {
   double last_ms = 0.;
   uint64_t max_events = 10000000ull;
   int prec = ABX_PREC_FP64;
+  void* flush = nullptr;
+  size_t flush_bytes = 0;
 };
 
 static void ctx_free(abx_ctx* c) {
@@ -650,7 +652,7 @@ static void ctx_free(abx_ctx* c) {
   c->sf.free_();
   void* ps[] = {c->tally_gen, c->tally_avg, c->tally_var, c->st, c->run, c->gen_rec,
                 c->ent_bins, c->ent_total, c->hist_count, c->offsets, c->block_sums, c->sec,
-                c->aos_in, c->aos_out, c->trace};
+                c->aos_in, c->aos_out, c->trace, c->flush};
   for (void* p : ps)
     if (p) cudaFree(p);
   if (c->st_host) cudaFreeHost(c->st_host);
@@ -1349,6 +1351,19 @@ extern "C" int abx_transport_noalloc(abx_ctx* c, const abx_particle* bank_dev, s
   return ABX_OK;
 }
 
+extern "C" int abx_set_l2_flush(abx_ctx* c, size_t bytes) {
+  if (!c) return fail(ABX_ERR_INVALID, "bad arguments");
+  cudaSetDevice(c->device);
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (c->flush) cudaFree(c->flush);
+  c->flush = nullptr;
+  c->flush_bytes = 0;
+  if (!bytes) return ABX_OK;
+  CUDA_TRY(cudaMalloc(&c->flush, bytes));
+  c->flush_bytes = bytes;
+  return ABX_OK;
+}
+
 extern "C" int abx_last_transport_ms(abx_ctx* c, double* ms) {
   if (!c || !ms) return fail(ABX_ERR_INVALID, "bad arguments");
   *ms = c->last_ms;
@@ -1520,6 +1535,7 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
   int cur = 0;
   int active_tally = 0;
   for (int g = 1; g <= ngen; g++) {
+    if (c->flush_bytes) CUDA_TRY(cudaMemsetAsync(c->flush, g & 0xff, c->flush_bytes, c->stream));
     cudaEventRecord(evs[4 * (g - 1)], c->stream);
     k_step_begin<<<1, 1, 0, c->stream>>>(c->st, 0, 0., 0, 1);
     cudaEventRecord(evs[4 * (g - 1) + 1], c->stream);

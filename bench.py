@@ -202,6 +202,9 @@ def main():
     builder.seed = builder.seed + 7919 * rank  # independent replica per rank
     eng = Engine(builder.build(precision=args.precision), local)
 
+    # L2 flush between generations, outside each generation's timed events
+    from abeille_gb300 import abi as _abi
+    _abi.check(eng.lib.abx_set_l2_flush(eng.ctx, L2_FLUSH_BYTES), eng.lib)
     # warm-up generations (untimed)
     eng.run_power_iteration(max(args.warmup, 1), 0)
     if dist:
@@ -240,8 +243,11 @@ def main():
     alg = flights * b["flight"] + coll * b["collision"] + sites * b["site"]
     achieved = alg / (tr_ms / 1e3) / 1e9
     peak, src = peaks()
+    hist = sum(r["histories"] for r in recs) / max(len(recs), 1)
+    tph = TRAFFIC_PER_HISTORY.get((args.config, args.precision))
+    traffic = tph * hist if tph else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": TRAFFIC.get((args.config, args.precision)), "peak_source": src,
+            "traffic": traffic, "peak_source": src,
             "kernel": "transport_kernel", "algorithmic_bytes_per_launch": alg / max(len(recs), 1)}
     cpu = None
     if world == 1 and not args.no_cpu:
@@ -254,8 +260,9 @@ def main():
         "vs_baseline": None, "dtype": "f32-track/f64-tally" if args.precision == "mixed" else "f64",
         "data": "synthetic",
         "config": {"workload": f"config{args.config}", "histories_per_generation": npart,
-                   "tracking": "delta", "precision": args.precision, "l2": "inputs larger than L2 "
-                   "(bank + fission bank ~0.3 GB per generation)", "parallelism": f"replicas{world}"},
+                   "tracking": "delta", "precision": args.precision,
+                   "l2": f"flushed: {L2_FLUSH_BYTES >> 20} MiB written before each generation, outside its "
+                   "timed events", "parallelism": f"replicas{world}"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": KERNELS_PER_GEN * args.steps,
         "clocks": clk.summary(),
@@ -268,8 +275,11 @@ def main():
     return 0
 
 
-# dram bytes per transport launch from the ncu captures summarised under profiles/
-TRAFFIC = {}
+# DRAM bytes (read + write) per history of a transport launch, from the ncu
+# capture in profiles/transport_kernel_config1_mixed_300k.md (16.27 MB at
+# 300,000 histories); the bank and site traffic grows with the histories.
+TRAFFIC_PER_HISTORY = {(1, "mixed"): 16.27e6 / 3e5}
+L2_FLUSH_BYTES = 256 << 20
 
 if __name__ == "__main__":
     sys.exit(main())

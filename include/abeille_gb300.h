@@ -379,6 +379,12 @@ int abx_get_trace(abx_ctx* ctx, abx_trace_rec* out, size_t capacity, size_t* n_o
 /* Device time of the most recent transport launch, in milliseconds. */
 int abx_last_transport_ms(abx_ctx* ctx, double* ms);
 
+/* Timing hygiene for benchmarks (no reference counterpart): before each
+ * generation of abx_run_power_iteration[_ex], outside the generation's timed
+ * events, write `bytes` of a private device buffer so that the L2 cache holds
+ * none of the previous generation's data.  0 (the default) turns it off. */
+int abx_set_l2_flush(abx_ctx* ctx, size_t bytes);
+
 #ifdef __cplusplus
 }
 #endif
