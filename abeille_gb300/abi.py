@@ -139,6 +139,12 @@ class GenRecord(C.Structure):
                 ("histories", C.c_uint64), ("sites", C.c_uint64), ("lost", C.c_uint64)]
 
 
+class ProblemResult(C.Structure):
+    _fields_ = [("leak_avg", C.c_double), ("leak_std", C.c_double), ("collisions", C.c_uint64),
+                ("flights", C.c_uint64), ("histories", C.c_uint64), ("lost", C.c_uint64), ("batches", C.c_int32),
+                ("tally_first", C.c_int32)]
+
+
 # every entry point declared in include/abeille_gb300.h, with its argument types
 PROTOTYPES = {
     "abx_create": (C.c_int, [C.POINTER(Problem), C.c_int, C.POINTER(C.c_void_p)]),
@@ -165,6 +171,8 @@ PROTOTYPES = {
     "abx_get_trace": (C.c_int, [C.c_void_p, C.POINTER(TraceRec), C.c_size_t, C.POINTER(C.c_size_t)]),
     "abx_last_transport_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "abx_set_l2_flush": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "abx_create_batch": (C.c_int, [C.POINTER(Problem), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "abx_run_fixed_source_batch": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(ProblemResult), C.POINTER(RunStats)]),
 }
 
 _lib = None

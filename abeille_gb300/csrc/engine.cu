@@ -639,6 +639,16 @@ struct abx_context {
   int prec = ABX_PREC_FP64;
   void* flush = nullptr;
   size_t flush_bytes = 0;
+  // batches of problems
+  int nprob = 1;
+  bool batch_scores = false;  // transport launches score per problem
+  double* pscore = nullptr;
+  unsigned long long* pcount = nullptr;
+  void* prun = nullptr;
+  uint64_t* seg_off = nullptr;
+  int32_t* seg_prob = nullptr;
+  uint64_t* seg_hid0 = nullptr;
+  int seg_batches = 0;
 };
 
 static void ctx_free(abx_ctx* c) {
@@ -652,7 +662,8 @@ static void ctx_free(abx_ctx* c) {
   c->sf.free_();
   void* ps[] = {c->tally_gen, c->tally_avg, c->tally_var, c->st, c->run, c->gen_rec,
                 c->ent_bins, c->ent_total, c->hist_count, c->offsets, c->block_sums, c->sec,
-                c->aos_in, c->aos_out, c->trace, c->flush};
+                c->aos_in, c->aos_out, c->trace, c->flush, c->pscore, c->pcount, c->prun,
+                c->seg_off, c->seg_prob, c->seg_hid0};
   for (void* p : ps)
     if (p) cudaFree(p);
   if (c->st_host) cudaFreeHost(c->st_host);
@@ -873,6 +884,30 @@ __global__ void k_gen_end(DevState* st, RunAcc* run, const ProbT* probs, abx_gen
   }
 }
 
+// Per-problem batch statistics of a batch context: the leakage estimator of
+// Tallies::calc_gen_values / record_generation (src/tallies.cpp:159-203,
+// 268-280) for every problem, then the per-problem sums are cleared.
+struct ProbRun {
+  double leak_avg, leak_var;
+  unsigned long long coll, flights, hist, lost;
+};
+__global__ void k_prob_record(double* ps, unsigned long long* pc, ProbRun* pr, const ProbT* probs, int np,
+                              int batch) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    double* s = ps + (size_t)p * ABX_PSCORES;
+    unsigned long long* c = pc + (size_t)p * ABX_PCOUNTS;
+    ProbRun r = pr[p];
+    upd(batch, s[3] / probs[p].nparticles, r.leak_avg, r.leak_var);
+    r.coll += c[0];
+    r.flights += c[1];
+    r.hist += c[2];
+    r.lost += c[3];
+    pr[p] = r;
+    for (int k = 0; k < ABX_PSCORES; k++) s[k] = 0.;
+    for (int k = 0; k < ABX_PCOUNTS; k++) c[k] = 0ull;
+  }
+}
+
 // MeshTally::record_generation + clear_generation (src/mesh_tally.cpp:121-152)
 __global__ void k_tally_record(double* gen, double* avg, double* var, size_t n, double mult, int rec,
                                double dg) {
@@ -1024,6 +1059,8 @@ template <class R> static TransportArgs<R> make_args(abx_ctx* c, const BankT<R>&
   A.trace_nhist = c->trace_nhist;
   A.trace_cap = c->trace_cap;
   A.max_events = c->max_events;
+  A.pscore = c->batch_scores ? c->pscore : nullptr;
+  A.pcount = c->batch_scores ? c->pcount : nullptr;
   return A;
 }
 
@@ -1055,15 +1092,27 @@ static unsigned grid_for(size_t n) {
 }
 
 // ------------------------------------------------------------------- C-ABI
-extern "C" int abx_create(const abx_problem* problem, int device, abx_ctx** out) {
+static int create_ctx(const abx_problem* problems, int nprob, int device, abx_ctx** out) {
   if (!out) return fail(ABX_ERR_INVALID, "null output pointer");
   *out = nullptr;
+  if (!problems || nprob <= 0) return fail(ABX_ERR_INVALID, "no problems");
+  const abx_problem* problem = &problems[0];
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(ABX_ERR_CUDA, "no CUDA device available");
   if (device < 0 || device >= ndev) return fail(ABX_ERR_INVALID, "device %d out of range", device);
   abx_ctx* c = new abx_context();
   c->device = device;
-  int rc = append_problem(c->P, problem);
+  c->nprob = nprob;
+  int rc = ABX_OK;
+  for (int i = 0; i < nprob && rc == ABX_OK; i++) {
+    const abx_settings& s = problems[i].settings;
+    if (nprob > 1 && (s.mode != ABX_MODE_FIXED_SOURCE || s.tracking != problem->settings.tracking ||
+                      s.precision != problem->settings.precision))
+      rc = fail(ABX_ERR_UNSUPPORTED,
+                "problem %d: a batch holds fixed-source problems of one tracking mode and one precision", i);
+    else
+      rc = append_problem(c->P, &problems[i]);
+  }
   if (rc) {
     delete c;
     return rc;
@@ -1116,6 +1165,18 @@ extern "C" int abx_create(const abx_problem* problem, int device, abx_ctx** out)
   if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(ABX_ERR_CUDA, "device sync failed"));
   *out = c;
   return ABX_OK;
+}
+
+extern "C" int abx_create(const abx_problem* problem, int device, abx_ctx** out) {
+  if (!problem) {
+    if (out) *out = nullptr;
+    return fail(ABX_ERR_INVALID, "null problem");
+  }
+  return create_ctx(problem, 1, device, out);
+}
+
+extern "C" int abx_create_batch(const abx_problem* problems, int n_problems, int device, abx_ctx** out) {
+  return create_ctx(problems, n_problems, device, out);
 }
 
 extern "C" int abx_destroy(abx_ctx* c) {
@@ -1691,6 +1752,145 @@ extern "C" int abx_run_fixed_source(abx_ctx* c, int nbatches, uint64_t npart, ab
     stats->histories = ra.total_hist;
     stats->transport_ms = tms;
     stats->total_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  }
+  return ABX_OK;
+}
+
+// Batch b of every problem of a batch context in one transport launch; the
+// per-batch bookkeeping of FixedSource::run (src/fixed_source.cpp:105-150)
+// for every problem at once.
+extern "C" int abx_run_fixed_source_batch(abx_ctx* c, int nbatches, abx_problem_result* results,
+                                          abx_run_stats* stats) {
+  if (!c || nbatches <= 0) return fail(ABX_ERR_INVALID, "bad arguments");
+  if (c->prob0.mode != ABX_MODE_FIXED_SOURCE) return fail(ABX_ERR_INVALID, "problem is not fixed-source");
+  cudaSetDevice(c->device);
+  const bool mixed = mixed_of(c);
+  const int np = c->nprob;
+  std::vector<uint64_t> off((size_t)np + 1);
+  std::vector<int32_t> pid((size_t)np);
+  uint64_t total = 0;
+  for (int p = 0; p < np; p++) {
+    off[p] = total;
+    pid[p] = p;
+    total += (uint64_t)c->P.probs[p].nparticles;
+  }
+  off[np] = total;
+  if (total == 0 || total > 0xffffffffull) return fail(ABX_ERR_CAPACITY, "%llu histories per batch", (unsigned long long)total);
+  for (int p = 0; p < np; p++) {
+    if (c->P.probs[p].src_count <= 0) return fail(ABX_ERR_INVALID, "problem %d has no sources", p);
+  }
+  int rc;
+  if ((rc = ensure_banks(c, total, mixed, true)) != ABX_OK) return rc;
+  if ((rc = ensure_sites(c, 1, mixed)) != ABX_OK) return rc;
+  if ((rc = ensure_sec(c, mixed)) != ABX_OK) return rc;
+  if ((rc = ensure_records(c, nbatches)) != ABX_OK) return rc;
+  if (!c->pscore) {
+    CUDA_TRY(cudaMalloc(&c->pscore, (size_t)np * ABX_PSCORES * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&c->pcount, (size_t)np * ABX_PCOUNTS * sizeof(unsigned long long)));
+    CUDA_TRY(cudaMalloc(&c->prun, (size_t)np * sizeof(ProbRun)));
+    CUDA_TRY(cudaMalloc(&c->seg_off, ((size_t)np + 1) * sizeof(uint64_t)));
+    CUDA_TRY(cudaMalloc(&c->seg_prob, (size_t)np * sizeof(int32_t)));
+  }
+  if (c->seg_batches < nbatches) {
+    if (c->seg_hid0) cudaFree(c->seg_hid0);
+    c->seg_hid0 = nullptr;
+    CUDA_TRY(cudaMalloc(&c->seg_hid0, (size_t)nbatches * np * sizeof(uint64_t)));
+    c->seg_batches = nbatches;
+  }
+  // first history id of batch b of problem p: b * n_p (src/fixed_source.cpp:152-155)
+  std::vector<uint64_t> hid0((size_t)nbatches * np);
+  for (int b = 0; b < nbatches; b++)
+    for (int p = 0; p < np; p++) hid0[(size_t)b * np + p] = (uint64_t)b * (off[p + 1] - off[p]);
+  CUDA_TRY(cudaMemcpyAsync(c->seg_off, off.data(), off.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(c->seg_prob, pid.data(), pid.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(c->seg_hid0, hid0.data(), hid0.size() * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                           c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->st, 0, sizeof(DevState), c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->run, 0, sizeof(RunAcc), c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->pscore, 0, (size_t)np * ABX_PSCORES * sizeof(double), c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->pcount, 0, (size_t)np * ABX_PCOUNTS * sizeof(unsigned long long), c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->prun, 0, (size_t)np * sizeof(ProbRun), c->stream));
+  zero_d(c->tally_gen, (size_t)c->P.tally_bins, c->stream);
+  zero_d(c->tally_avg, (size_t)c->P.tally_bins, c->stream);
+  zero_d(c->tally_var, (size_t)c->P.tally_bins, c->stream);
+  c->tally_g = 0;
+  std::vector<cudaEvent_t> evs(4 * (size_t)nbatches);
+  for (auto& e : evs) cudaEventCreate(&e);
+  c->batch_scores = true;
+  for (int b = 0; b < nbatches; b++) {
+    cudaEventRecord(evs[4 * b], c->stream);
+    SourceArgs S{};
+    S.T = c->D.T;
+    S.n = total;
+    BankT<double>& b0 = c->bd[0].b;
+    S.x = b0.x; S.y = b0.y; S.z = b0.z; S.ux = b0.ux; S.uy = b0.uy; S.uz = b0.uz; S.E = b0.E; S.w = b0.w;
+    S.w2 = b0.w2; S.rng = b0.rng; S.hid = b0.hid; S.fam = b0.fam; S.probv = b0.prob; S.out_off = 0; S.st = c->st;
+    S.seg_off = c->seg_off;
+    S.seg_prob = c->seg_prob;
+    S.seg_hid0 = c->seg_hid0 + (size_t)b * np;
+    S.nseg = np;
+    launch_sources(S, c->stream);
+    if (mixed) k_bank_d2f<<<grid_for(total), 256, 0, c->stream>>>(b0, c->bf[0].b, 0, total);
+    k_step_begin<<<1, 1, 0, c->stream>>>(c->st, total, 1.0, 1, 0);
+    cudaEventRecord(evs[4 * b + 1], c->stream);
+    if ((rc = launch_transport(c, mixed, 0, 0)) != ABX_OK) break;
+    cudaEventRecord(evs[4 * b + 2], c->stream);
+    if (c->P.tally_bins)
+      k_tally_record<<<grid_for((size_t)c->P.tally_bins), 256, 0, c->stream>>>(
+          c->tally_gen, c->tally_avg, c->tally_var, (size_t)c->P.tally_bins, 1.0, 1, (double)(b + 1));
+    k_prob_record<<<(np + 255) / 256, 256, 0, c->stream>>>(c->pscore, c->pcount, (ProbRun*)c->prun, c->D.T.probs,
+                                                           np, b + 1);
+    k_gen_end<<<1, 1024, 0, c->stream>>>(c->st, c->run, c->D.T.probs, c->gen_rec, c->hist_cap, c->ent_bins,
+                                         nullptr, 0, total, 0, 0);
+    cudaEventRecord(evs[4 * b + 3], c->stream);
+    if (cudaGetLastError() != cudaSuccess) {
+      rc = fail(ABX_ERR_CUDA, "launch failed");
+      break;
+    }
+    if ((b & 7) == 7 || b == nbatches - 1)
+      if ((rc = check_state(c)) != ABX_OK) break;
+  }
+  c->batch_scores = false;
+  if (rc == ABX_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = fail(ABX_ERR_CUDA, "stream sync failed");
+  double tms = 0., sms = 0.;
+  for (int b = 0; b < nbatches && rc == ABX_OK; b++) {
+    float ms = 0.f, ts = 0.f;
+    cudaEventElapsedTime(&ms, evs[4 * b], evs[4 * b + 3]);
+    cudaEventElapsedTime(&ts, evs[4 * b + 1], evs[4 * b + 2]);
+    sms += ms;
+    tms += ts;
+  }
+  for (auto& e : evs) cudaEventDestroy(e);
+  if (rc) return rc;
+  c->tally_g = nbatches;
+  c->last_ms = tms;
+  std::vector<ProbRun> pr((size_t)np);
+  CUDA_TRY(cudaMemcpy(pr.data(), c->prun, (size_t)np * sizeof(ProbRun), cudaMemcpyDeviceToHost));
+  RunAcc ra;
+  CUDA_TRY(cudaMemcpy(&ra, c->run, sizeof ra, cudaMemcpyDeviceToHost));
+  if (results) {
+    for (int p = 0; p < np; p++) {
+      abx_problem_result& r = results[p];
+      memset(&r, 0, sizeof r);
+      r.leak_avg = pr[p].leak_avg;
+      r.leak_std = std::sqrt(pr[p].leak_var / nbatches);
+      r.collisions = pr[p].coll;
+      r.flights = pr[p].flights;
+      r.histories = pr[p].hist;
+      r.lost = pr[p].lost;
+      r.batches = nbatches;
+      r.tally_first = c->P.probs[p].tally_first;
+    }
+  }
+  if (stats) {
+    memset(stats, 0, sizeof *stats);
+    stats->generations = ra.gen;
+    stats->active = ra.active;
+    stats->collisions = ra.total_coll;
+    stats->flights = ra.total_flights;
+    stats->histories = ra.total_hist;
+    stats->transport_ms = tms;
+    stats->total_ms = sms;
   }
   return ABX_OK;
 }

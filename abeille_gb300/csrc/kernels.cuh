@@ -1,16 +1,11 @@
-// Transport kernels of the GB300 multigroup engine, templated on the tracking
-// precision R.  Included by transport_fp64.cu (R = double, --fmad=false) and
-// transport_mixed.cu (R = float).
+// Device building blocks of the transport loop, templated on the tracking
+// precision R: argument and bank layouts, score accumulators, the collision
+// (Transporter::collision and its helpers) and the mesh-tally estimators.
+// Included by transport_loop.cuh, which transport_fp64.cu (R = double,
+// --fmad=false) and transport_mixed.cu (R = float) instantiate.
 //
-// Design: one persistent launch per transport call.  Each lane owns one
-// history at a time with its whole state (position, direction, weight, pcg32
-// state and the geometry tree) in registers.  A lane whose history ends takes
-// the next one from a global work counter (warp-aggregated), so lanes never
-// wait for a slow neighbour ("lane refill"); every loop iteration advances
-// each lane by exactly one flight, plus one collision when the flight ends in
-// a real collision.  Fission sites are appended with warp-aggregated atomics
-// and keyed by (history, daughter) so a counting sort restores the
-// reference's bank order.
+// Fission sites are appended with warp-aggregated atomics and keyed by
+// (history, daughter) so a counting sort restores the reference's bank order.
 #pragma once
 
 #include <cooperative_groups.h>
@@ -50,7 +45,13 @@ template <class R> struct TransportArgs {
   uint32_t trace_nhist;
   uint64_t trace_cap;
   uint64_t max_events;
+  // batches of problems: per-problem score sums [prob][ABX_PSCORES] and
+  // counters [prob][ABX_PCOUNTS]; nullptr when one problem runs alone
+  double* pscore;
+  unsigned long long* pcount;
 };
+
+enum : int { ABX_PSCORES = 5, ABX_PCOUNTS = 4 };  // counters: collisions flights histories lost
 
 template <class R> ABX_DEV View<R> make_view(const Tables& T);
 template <> ABX_DEV View<double> make_view<double>(const Tables& T) {
@@ -74,7 +75,8 @@ template <> ABX_DEV void tally_geom<float>(const TallyT& t, float low[3], float 
 // Score accumulators.  Each history sums its terms in the tracking precision;
 // at the end of the history the five totals are added, in FP64, to the block's
 // shared accumulators (one FP64 atomic each), which the block adds to the
-// global scores when it retires.  In FP64 mode every term is a double, so
+// global scores when it retires; in a batch of problems they go straight to
+// the history's own problem.  In FP64 mode every term is a double, so
 // the sums are FP64 throughout, as the reference's ThreadLocalScores.
 template <class R> struct Acc {
   R hcol = 0, habs = 0, htrk = 0, hleak = 0, hmig = 0;
@@ -98,7 +100,8 @@ template <class R> struct Lane {
   int mat;
   uint32_t dau;
   uint32_t nsec;
-  uint32_t events;
+  uint32_t events;  // flights of this history (secondaries included)
+  uint32_t hcoll;   // real collisions of this history
   uint32_t npos, nneg;
 };
 

@@ -23,6 +23,13 @@ struct SourceArgs {
   int32_t* probv;           // optional per-history problem index output
   uint64_t out_off;         // write offset into the output arrays
   DevState* st;
+  // batches of problems: output index i belongs to segment s with
+  // seg_off[s] <= i < seg_off[s+1]: problem seg_prob[s], history id
+  // seg_hid0[s] + (i - seg_off[s]).  nseg == 0: one problem (prob, first_hid).
+  const uint64_t* seg_off;
+  const int32_t* seg_prob;
+  const uint64_t* seg_hid0;
+  int nseg;
 };
 
 // transport_fp64.cu

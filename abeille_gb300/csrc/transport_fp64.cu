@@ -39,10 +39,21 @@ int transport_regs_d(int tracking) {
 __global__ void __launch_bounds__(128) sources_kernel(const SourceArgs A) {
   const Tables& T = A.T;
   const View<double> V = make_view<double>(T);
-  const ProbT& P = T.probs[A.prob];
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < A.n;
        i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t hid = A.first_hid + i;
+    int prob = A.prob;
+    uint64_t hid = A.first_hid + i;
+    if (A.nseg > 0) {
+      // last segment whose first index is <= i
+      int lo = 0, hi = A.nseg - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.seg_off[mid] <= i) lo = mid; else hi = mid - 1;
+      }
+      prob = A.seg_prob[lo];
+      hid = A.seg_hid0[lo] + (i - A.seg_off[lo]);
+    }
+    const ProbT& P = T.probs[prob];
     uint64_t rng = pcg_advance(pcg_seeded(P.seed), P.stride * hid);
     int si = P.src_first + discrete<double>(rng, T.src_cdf + P.src_cdf_off, P.src_count);
     const abx_source S = T.sources[si];
@@ -100,7 +111,7 @@ __global__ void __launch_bounds__(128) sources_kernel(const SourceArgs A) {
     A.E[o] = E; A.w[o] = 1.0; A.w2[o] = 0.;
     A.rng[o] = rng; A.hid[o] = hid;
     if (A.fam) A.fam[o] = hid;
-    if (A.probv) A.probv[o] = A.prob;
+    if (A.probv) A.probv[o] = prob;
   }
 }
 

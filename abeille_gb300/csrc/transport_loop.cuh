@@ -49,6 +49,7 @@ ABX_DEV bool lane_load(const TransportArgs<R>& A, const Tables& T, const View<R>
   L.dau = 0;
   L.nsec = 0;
   L.events = 0;
+  L.hcoll = 0;
   const ProbT& P = T.probs[L.pid];
   L.g = group_of<R>(V.ebnd + P.eb_off, P.G, L.E);
   k.r = L.r;
@@ -87,6 +88,23 @@ ABX_DEV void reflect_move(const View<R>& V, Trk<R>& k, Lane<R>& L, const Bound<R
   trk_set_r(k, L.r);
   k.u = L.u;
   if (sizeof(R) == 4) k.token = side;
+}
+
+// End of a history: its fission-site count (for the bank sort) and its score
+// totals, to the block's accumulators or, in a batch of problems, to its
+// problem's sums and counters.
+template <class R>
+ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& acc, double* sh_acc) {
+  A.hist_count[L.h] = L.dau;
+  if (A.pscore) {
+    acc.flush(A.pscore + (size_t)L.pid * ABX_PSCORES);
+    unsigned long long* c = A.pcount + (size_t)L.pid * ABX_PCOUNTS;
+    atomicAdd(c + 0, (unsigned long long)L.hcoll);
+    atomicAdd(c + 1, (unsigned long long)L.events);
+    atomicAdd(c + 2, 1ull);
+  } else {
+    acc.flush(sh_acc);
+  }
 }
 
 template <class R, int TRACK>
@@ -130,6 +148,11 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
     raise_err(st, (code), L.h);   \
     done = true;                  \
     ph = PH_DONE;                 \
+  }
+#define ABX_LOST()                                                                              \
+  {                                                                                             \
+    nlost++;                                                                                    \
+    if (A.pcount) atomicAdd(A.pcount + (size_t)L.pid * ABX_PCOUNTS + 3, 1ull);                  \
   }
 
   while (true) {
@@ -245,8 +268,8 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
     // ------------------------------------------------ post-descend checks
     if (ph == PH_START) {
       if (k.cell < 0) {  // lost at birth: a warning in the reference, the particle is killed
-        nlost++;
-        A.hist_count[L.h] = 0;
+        ABX_LOST();
+        history_end(A, L, acc, sh_acc);
         ph = PH_REFILL;
       } else {
         L.mat = T.cells[k.cell].fill;
@@ -261,7 +284,7 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
     } else if (ph == PH_REFL) {
       if (k.cell < 0) {
         if (sizeof(R) == 8) ABX_FAIL(ABX_ERR_LOST_PARTICLE) else {
-          nlost++;  // mixed mode: counted in `lost` and killed
+          ABX_LOST();  // mixed mode: counted in `lost` and killed
           ph = PH_DEAD;
         }
       } else {
@@ -279,7 +302,7 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
         ph = PH_WAIT;
       } else if (k.cell < 0) {
         if (sizeof(R) == 8) ABX_FAIL(ABX_ERR_LOST_PARTICLE) else {
-          nlost++;
+          ABX_LOST();
           ph = PH_DEAD;
         }
       } else {
@@ -333,7 +356,7 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
       } else if (sizeof(R) == 8) {
         ABX_FAIL(ABX_ERR_LOST_PARTICLE);
       } else {
-        nlost++;
+        ABX_LOST();
         ph = PH_DEAD;
       }
     }
@@ -343,6 +366,7 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
       const ProbT& P = T.probs[L.pid];
       bool alive = true;
       ncoll++;
+      L.hcoll++;
       collide(A, T, V, P, L, acc, converged, kcol, alive);
       k.u = L.u;
       if (TRACE) trace_rec(A, L, 4, k.cell);
@@ -371,8 +395,7 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
           ph = PH_WAIT;
         }
       } else {
-        A.hist_count[L.h] = L.dau;
-        acc.flush(sh_acc);
+        history_end(A, L, acc, sh_acc);
         ph = PH_REFILL;
       }
     }
@@ -381,9 +404,8 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
       if (sizeof(R) == 4) {
         // mixed mode: a history this long is a geometry rounding trap, not
         // physics; it is counted in `lost` and ended
-        nlost++;
-        A.hist_count[L.h] = L.dau;
-        acc.flush(sh_acc);
+        ABX_LOST();
+        history_end(A, L, acc, sh_acc);
         ph = PH_REFILL;
       } else {
         ABX_FAIL(ABX_ERR_TIMEOUT);
@@ -391,6 +413,7 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
     }
   }
 #undef ABX_FAIL
+#undef ABX_LOST
   acc.flush(sh_acc);
   unsigned long long c[5] = {ncoll, nflight, nlost, (unsigned long long)L.npos, (unsigned long long)L.nneg};
 #pragma unroll

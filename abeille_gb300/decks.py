@@ -221,16 +221,19 @@ def config2(nparticles=2000000, precision="fp64", tracking="surface-tracking"):
     return b
 
 
-def fixed_source_problem(index, seed=3, precision="mixed", nparticles=None, tracking="delta-tracking"):
+def fixed_source_problem(index, seed=3, precision="mixed", nparticles=None, tracking="delta-tracking", batches=10):
     """One config-3 problem: a box of 1-4 slabs along x (thickness log-uniform
     1-50 cm), G in {7, 22, 44}, sigma_t in [0.05, 5], scattering ratio in
     [0.3, 0.99], isotropic point source at the centre in group 0, 20x20x20
-    collision flux tally, vacuum on every side.  Histories log-uniform 1e3-1e5."""
+    collision flux tally, vacuum on every side.  Histories log-uniform 1e3-1e5
+    in total, run as `batches` batches of nparticles = total / batches (at
+    least 1) each; `nparticles` overrides the per-batch count."""
     rng = np.random.default_rng([seed, index])
     G = int(rng.choice([7, 22, 44]))
     nl = int(rng.integers(1, 5))
     th = np.exp(rng.uniform(np.log(1.0), np.log(50.0), nl))
-    hist = int(round(np.exp(rng.uniform(np.log(1e3), np.log(1e5)))))
+    total = np.exp(rng.uniform(np.log(1e3), np.log(1e5)))
+    hist = max(1, int(round(total / batches)))
     if nparticles is not None:
         hist = nparticles
     width = th.sum()

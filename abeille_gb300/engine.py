@@ -132,6 +132,29 @@ class Engine:
         return out
 
 
+class BatchEngine(Engine):
+    """Many fixed-source problems resident on one GPU; batch b of every
+    problem is transported in one launch, and each problem's results are those
+    of FixedSource::run for it alone."""
+
+    def __init__(self, builts, device=0):
+        self.lib = abi.load()
+        self.builts = list(builts)
+        self.built = self.builts[0]
+        arr = (abi.Problem * len(self.builts))(*[b.struct for b in self.builts])
+        self._arr = arr
+        self.ctx = C.c_void_p()
+        abi.check(self.lib.abx_create_batch(arr, len(self.builts), device, C.byref(self.ctx)), self.lib)
+
+    def run(self, nbatches):
+        """Returns (per-problem result dicts, run totals)."""
+        res = (abi.ProblemResult * len(self.builts))()
+        st = abi.RunStats()
+        self._chk(self.lib.abx_run_fixed_source_batch(self.ctx, nbatches, res, C.byref(st)))
+        rows = [{f: getattr(r, f) for f, _ in abi.ProblemResult._fields_} for r in res]
+        return rows, stats_dict(st)
+
+
 class _GpuTracker:
     """Transporter::transport on the GPU: consumes the bank, returns the
     fission bank in BankedParticle::operator< order."""

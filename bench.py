@@ -188,9 +188,15 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=200000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tracking", default=None, choices=["delta-tracking", "surface-tracking"])
+    ap.add_argument("--problems", type=int, default=4096, help="config 3: problems in the batch")
+    ap.add_argument("--per-problem-sample", type=int, default=128,
+                    help="config 3: problems timed one launch per problem")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == 3:
+        return bench_batch(args)
 
     import __graft_entry__
     __graft_entry__.build()
@@ -199,6 +205,8 @@ def main():
     rank, world, local, dist = dist_setup(args.gpus)
     npart = args.particles or {0: 10000, 1: 1000000, 2: 2000000}[args.config]
     builder = decks.CONFIGS[args.config](nparticles=npart)
+    if args.tracking:
+        builder.tracking = args.tracking
     builder.seed = builder.seed + 7919 * rank  # independent replica per rank
     eng = Engine(builder.build(precision=args.precision), local)
 
@@ -260,7 +268,7 @@ def main():
         "vs_baseline": None, "dtype": "f32-track/f64-tally" if args.precision == "mixed" else "f64",
         "data": "synthetic",
         "config": {"workload": f"config{args.config}", "histories_per_generation": npart,
-                   "tracking": "delta", "precision": args.precision,
+                   "tracking": builder.tracking, "precision": args.precision,
                    "l2": f"flushed: {L2_FLUSH_BYTES >> 20} MiB written before each generation, outside its "
                    "timed events", "parallelism": f"replicas{world}"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
@@ -268,6 +276,131 @@ def main():
         "clocks": clk.summary(),
         "detail": {"flights": flights, "collisions": coll, "sites": sites, "transport_ms": tr_ms,
                    "wall_s": wall, "kcol_last": recs[-1]["kcol"], "lost": sum(r["lost"] for r in recs)},
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+    return 0
+
+
+def bench_batch(args):
+    """Config 3: `--problems` independent fixed-source slab problems resident
+    together; one step = batch b of every problem in one transport launch
+    (plus source sampling and the per-problem records).  Beside it, a sample
+    of the same problems run one problem per launch (their own context and
+    FixedSource loop each), in the same precision and in FP64."""
+    import __graft_entry__
+    __graft_entry__.build()
+    import numpy as np
+    from abeille_gb300 import BatchEngine, Engine, decks
+
+    rank, world, local, dist = dist_setup(args.gpus)
+    nb = args.steps
+    builders = [decks.fixed_source_problem(i, seed=3 + rank, precision=args.precision, batches=nb)
+                for i in range(args.problems)]
+    if args.tracking:
+        for b in builders:
+            b.tracking = args.tracking
+    builts = [b.build(precision=args.precision) for b in builders]
+    hist_per_batch = sum(b.nparticles for b in builders)
+
+    warm = BatchEngine(builts, local)
+    warm.run(max(args.warmup, 1))
+    warm.close()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    eng = BatchEngine(builts, local)
+    t_create = time.perf_counter() - t0
+    with Clocks(local) as clk:
+        t1 = time.perf_counter()
+        rows, st = eng.run(nb)
+        t_run = time.perf_counter() - t1
+    # end to end: create (host tables + upload) + run + every problem's tally read back
+    t2 = time.perf_counter()
+    d2h = 0
+    for r in rows:
+        t = eng.tally(r["tally_first"])
+        d2h += t["avg"].nbytes + t["var"].nbytes + t["gen"].nbytes
+    t_read = time.perf_counter() - t2
+    e2e_wall = t_create + t_run + t_read
+    h2d = sum(sum(getattr(a, "nbytes", 0) for a in b._keep) for b in builts)
+    coll, flights = st["collisions"], st["flights"]
+    step_ms, tr_ms = st["total_ms"], st["transport_ms"]
+    if dist:
+        import torch
+        t = torch.tensor([step_ms / 1e3, float(coll)], dtype=torch.float64, device=f"cuda:{local}")
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        secs, coll_all = float(tmax[0]), float(t[1])
+    else:
+        secs, coll_all = step_ms / 1e3, float(coll)
+    eng.close()
+    if rank != 0:
+        if dist:
+            dist.barrier()
+        return 0
+
+    # one problem per launch, on an evenly spaced sample of the same problems
+    idx = np.linspace(0, args.problems - 1, min(args.per_problem_sample, args.problems)).astype(int)
+    per = {}
+    for prec in sorted({args.precision, "fp64"}):
+        c_sum, wall, dev = 0, 0.0, 0.0
+        for i in idx:
+            b = decks.fixed_source_problem(int(i), seed=3, precision=prec, batches=nb)
+            if args.tracking:
+                b.tracking = args.tracking
+            e = Engine(b.build(precision=prec), local)
+            ta = time.perf_counter()
+            s1 = e.run_fixed_source(nb, b.nparticles)
+            wall += time.perf_counter() - ta
+            dev += s1["transport_ms"] / 1e3
+            c_sum += s1["collisions"]
+            e.close()
+        per[prec] = {"value": c_sum / wall, "transport_only_value": c_sum / dev, "unit": "collisions/s",
+                     "problems": len(idx), "precision": prec}
+    b = BYTES[args.precision]
+    alg = flights * b["flight"] + coll * b["collision"]
+    peak, src = peaks()
+    roof = {"bound": "hbm", "achieved": alg / (tr_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": alg / (tr_ms / 1e3) / 1e9 / peak, "traffic": None, "peak_source": src,
+            "kernel": "transport_kernel", "algorithmic_bytes_per_launch": alg / nb}
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        import oracle
+        c_sum, secs_cpu, used = 0, 0.0, 0
+        for i in idx:
+            bo = decks.fixed_source_problem(int(i), seed=3, precision="fp64", batches=nb)
+            o = oracle.Oracle(bo.build(precision="fp64"), nthreads=oracle.cores())
+            ta = time.perf_counter()
+            so = o.run_fixed_source(nb, bo.nparticles)
+            secs_cpu += time.perf_counter() - ta
+            c_sum += so["collisions"]
+            used += 1
+            if secs_cpu > 15.0:
+                break
+        cpu = {"value": c_sum / secs_cpu, "unit": "collisions/s", "cores": oracle.cores(), "kind": "port",
+               "sample": f"{used} of the problems, {nb} batches each, FP64, one problem at a time"}
+    line = {
+        "metric": "collisions/s", "value": coll_all / secs, "unit": "collisions/s", "n_gpus": world,
+        "steps": nb, "warmup": args.warmup, "ms_per_step": step_ms / nb, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-track/f64-tally" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": "config3", "problems": args.problems, "histories_per_step": hist_per_batch,
+                   "batches": nb, "tracking": builders[0].tracking, "precision": args.precision,
+                   "l2": "inputs larger than L2 (bank of all problems' batch, tallies of 4096x8000 bins)",
+                   "parallelism": f"replicas{world}"},
+        "roofline": roof, "cpu_baseline": cpu,
+        "e2e": {"value": coll_all / e2e_wall, "unit": "collisions/s", "h2d_bytes_per_step": h2d // nb,
+                "d2h_bytes_per_step": d2h // nb,
+                "what": "abx_create_batch + abx_run_fixed_source_batch + every tally read back, wall"},
+        "per_problem_launch": per,
+        "gpu_launches": (7 if args.precision == "mixed" else 6) * nb,
+        "clocks": clk.summary(),
+        "detail": {"collisions": coll, "flights": flights, "transport_ms": tr_ms, "create_s": t_create,
+                   "run_wall_s": t_run, "tally_read_s": t_read,
+                   "lost": int(sum(r["lost"] for r in rows))},
     }
     print(json.dumps(line), flush=True)
     if dist:

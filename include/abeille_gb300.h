@@ -358,6 +358,39 @@ int abx_run_power_iteration_ex(abx_ctx* ctx, int ngenerations, int nignored,
 int abx_run_fixed_source(abx_ctx* ctx, int nbatches, uint64_t nparticles,
                          abx_run_stats* stats);
 
+/* ------------------------------------------------- batches of problems */
+/* Many independent fixed-source problems in one context.  Each problem keeps
+ * its own geometry, materials, group structure, tallies, seed and stride, so
+ * its results are the ones FixedSource::run (src/fixed_source.cpp:81-173)
+ * gives for it alone: batch b of problem p transports histories
+ * b*n_p .. (b+1)*n_p-1 (n_p = its settings.nparticles), each seeded by
+ * skip-ahead on the problem's own stream.  The GPU transports batch b of
+ * every problem in one launch.  The reference runs one problem per process;
+ * this entry point has no single reference counterpart. */
+typedef struct abx_problem_result {
+  double leak_avg;          /* leakage per source particle, mean over batches */
+  double leak_std;          /* its standard deviation (of the mean)           */
+  uint64_t collisions;      /* summed over the problem's batches              */
+  uint64_t flights;
+  uint64_t histories;
+  uint64_t lost;
+  int32_t batches;
+  int32_t tally_first;      /* id of the problem's first mesh tally           */
+} abx_problem_result;
+
+/* Like abx_create for `n_problems` problems.  All must be fixed-source with
+ * the same tracking and precision (ABX_ERR_UNSUPPORTED otherwise).  Tally ids
+ * number the problems' tallies in problem order (`tally_first` above). */
+int abx_create_batch(const abx_problem* problems, int n_problems, int device, abx_ctx** out);
+
+/* Runs `nbatches` batches of every problem of a batch context; `results`
+ * (n_problems entries, may be NULL) receives each problem's scores, `stats`
+ * (may be NULL) the totals, the transport device time (`transport_ms`) and,
+ * in `total_ms`, the device time of the whole batches (source sampling,
+ * transport, tally and score records). */
+int abx_run_fixed_source_batch(abx_ctx* ctx, int nbatches, abx_problem_result* results,
+                               abx_run_stats* stats);
+
 /* -------------------------------------------------------- diagnostics */
 /* Per-event trace of the first `n_hist` histories of the next abx_transport
  * call (test hook).  Each record: history index, event kind, rng state,

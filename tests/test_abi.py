@@ -33,7 +33,8 @@ def test_struct_layouts_match_c():
                "abx_material": abi.Material, "abx_mesh_tally": abi.MeshTally, "abx_entropy_mesh": abi.EntropyMesh,
                "abx_source": abi.Source, "abx_settings": abi.Settings, "abx_problem": abi.Problem,
                "abx_particle": abi.Particle, "abx_site": abi.Site, "abx_scores": abi.Scores,
-               "abx_run_stats": abi.RunStats, "abx_trace_rec": abi.TraceRec}
+               "abx_run_stats": abi.RunStats, "abx_trace_rec": abi.TraceRec,
+               "abx_gen_record": abi.GenRecord, "abx_problem_result": abi.ProblemResult}
     src = '#include <stdio.h>\n#include <stddef.h>\n#include "abeille_gb300.h"\nint main(void){\n'
     for name in structs:
         src += f'printf("%zu\\n", sizeof({name}));\n'
