@@ -6,7 +6,7 @@ and provides the problem builder, synthetic decks and the reference-shaped
 Transporter / driver classes.
 """
 from . import abi, decks  # noqa: F401
-from .engine import (BatchEngine, Engine, FixedSource, GpuDeltaTracker, GpuSurfaceTracker, PowerIterator,  # noqa: F401
+from .engine import (BatchEngine, Engine, FixedSource, GpuDeltaTracker, GpuSurfaceTracker, PowerIterator, Server,  # noqa: F401
                      PARTICLE_DTYPE, SITE_DTYPE, TRACE_DTYPE)
 from .problem import ProblemBuilder, infix_to_rpn, tokenize_region  # noqa: F401
 

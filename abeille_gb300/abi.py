@@ -145,6 +145,23 @@ class ProblemResult(C.Structure):
                 ("tally_first", C.c_int32)]
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("tracking", C.c_int32), ("nbatches", C.c_int32),
+                ("hbm_budget_bytes", C.c_uint64), ("max_round_problems", C.c_int32), ("keep_tallies", C.c_int32)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("request_id", C.c_uint64), ("tag", C.c_uint64), ("status", C.c_int32), ("round", C.c_int32),
+                ("round_problems", C.c_int32), ("n_tallies", C.c_int32), ("n_tally_bins", C.c_uint64),
+                ("result", ProblemResult), ("queue_ms", C.c_double), ("latency_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("rounds", C.c_uint64), ("collisions", C.c_uint64), ("flights", C.c_uint64),
+                ("histories", C.c_uint64), ("busy_ms", C.c_double), ("transport_ms", C.c_double)]
+
+
 # every entry point declared in include/abeille_gb300.h, with its argument types
 PROTOTYPES = {
     "abx_create": (C.c_int, [C.POINTER(Problem), C.c_int, C.POINTER(C.c_void_p)]),
@@ -173,6 +190,14 @@ PROTOTYPES = {
     "abx_set_l2_flush": (C.c_int, [C.c_void_p, C.c_size_t]),
     "abx_create_batch": (C.c_int, [C.POINTER(Problem), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "abx_run_fixed_source_batch": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(ProblemResult), C.POINTER(RunStats)]),
+    "abx_tally_read_all": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "abx_server_create": (C.c_int, [C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
+    "abx_server_destroy": (C.c_int, [C.c_void_p]),
+    "abx_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.c_uint64, C.POINTER(C.c_uint64)]),
+    "abx_server_poll": (C.c_int, [C.c_void_p, C.POINTER(RequestResult), C.c_int, C.POINTER(C.c_int), C.c_int]),
+    "abx_server_tally": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_size_t]),
+    "abx_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "abx_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
 }
 
 _lib = None

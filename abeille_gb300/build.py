@@ -1,11 +1,12 @@
 """In-tree build of the CUDA engine (sm_103a) into abeille_gb300/_lib/.
 
-Three translation units are compiled in parallel with nvcc and linked into one
+Four translation units are compiled in parallel with nvcc and linked into one
 shared library exposing the C-ABI of include/abeille_gb300.h:
 
   engine.cu           host side + bookkeeping kernels     --fmad=false
   transport_fp64.cu   FP64 parity transport kernels        --fmad=false
   transport_mixed.cu  FP32-tracking transport kernels
+  server.cpp          request loop (host scheduler thread)
 
 Host code is compiled with -ffp-contract=off so derived tables round the same
 way on x86-64 and AArch64.  A stamp of the sources and flags skips rebuilds.
@@ -29,6 +30,7 @@ UNITS = [
     ("engine.cu", ["--fmad=false"]),
     ("transport_fp64.cu", ["--fmad=false"]),
     ("transport_mixed.cu", []),
+    ("server.cpp", []),
 ]
 
 
@@ -62,7 +64,7 @@ def build(force=False, verbose=False):
     cc = nvcc()
     objs, procs = [], []
     for src, extra in UNITS:
-        obj = os.path.join(LIBDIR, src.replace(".cu", ".o"))
+        obj = os.path.join(LIBDIR, os.path.splitext(src)[0] + ".o")
         cmd = [cc] + COMMON + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
@@ -78,7 +80,7 @@ def build(force=False, verbose=False):
     if failed:
         raise RuntimeError("nvcc failed:\n" + "\n".join(f"--- {s}\n{o}" for s, o in failed))
     tmp = LIB + ".tmp"
-    subprocess.check_call([cc] + ARCH + ["-shared", "-o", tmp] + objs)
+    subprocess.check_call([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
     os.replace(tmp, LIB)
     with open(stamp_file, "w") as f:
         f.write(stamp)

@@ -42,6 +42,9 @@ static int fail(int code, const char* fmt, ...) {
   } while (0)
 
 extern "C" const char* abx_last_error_string(void) { return g_err.c_str(); }
+namespace abx {
+void set_error_string(const char* msg) { g_err = msg; }
+}
 extern "C" int abx_version(int* a, int* b, int* c) {
   if (a) *a = 0;
   if (b) *b = 4;
@@ -1474,6 +1477,19 @@ extern "C" int abx_tally_read(abx_ctx* c, int id, double* gen, double* avg, doub
   if (var) CUDA_TRY(cudaMemcpyAsync(var, c->tally_var + t.bin_off, n * 8, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   if (generations) *generations = c->tally_g;
+  return ABX_OK;
+}
+
+extern "C" int abx_tally_read_all(abx_ctx* c, double* avg, double* var, size_t capacity, size_t* n_bins) {
+  if (!c || !n_bins) return fail(ABX_ERR_INVALID, "bad arguments");
+  const size_t n = (size_t)c->P.tally_bins;
+  *n_bins = n;
+  if (!avg && !var) return ABX_OK;
+  if (capacity < n) return fail(ABX_ERR_CAPACITY, "%zu tally bins, capacity %zu", n, capacity);
+  cudaSetDevice(c->device);
+  if (avg && n) CUDA_TRY(cudaMemcpyAsync(avg, c->tally_avg, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (var && n) CUDA_TRY(cudaMemcpyAsync(var, c->tally_var, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
   return ABX_OK;
 }
 

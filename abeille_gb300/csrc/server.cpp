@@ -1,0 +1,367 @@
+// Request loop for fixed-source problems: a host scheduler over the C-ABI.
+//
+// Submission copies the problem (the caller's buffers are not retained) and
+// queues it with an estimate of its device footprint.  One scheduler thread
+// runs rounds: it admits queued requests in arrival order while the sum of
+// their footprints fits the HBM budget, creates one batch context for them,
+// runs every request's batches (batch b of all admitted problems in one
+// transport launch), copies results and tally bins back, and frees the
+// context.  Requests that arrive during a round wait for the next one, so the
+// rounds size themselves to the arrival rate.
+//
+// A request's results do not depend on its round: batch b of a problem
+// always transports its histories b*n .. (b+1)*n-1, each seeded by skip-ahead
+// on the problem's own stream, and its tallies and scores are its own.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "abeille_gb300.h"
+
+namespace abx {
+void set_error_string(const char* msg);  // engine.cu: the thread's abx_last_error_string
+}
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+int srv_fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  abx::set_error_string(buf);
+  return code;
+}
+
+// Deep copy of an abx_problem; `p` points into the vectors.
+struct ProblemCopy {
+  abx_problem p{};
+  std::vector<double> eb, mg, teb;
+  std::vector<abx_surface> surf;
+  std::vector<abx_cell> cells;
+  std::vector<int32_t> rpn, lists, lat;
+  std::vector<abx_universe> univ;
+  std::vector<abx_material> mats;
+  std::vector<abx_mesh_tally> tallies;
+  std::vector<abx_source> src;
+
+  template <class T> static void take(std::vector<T>& v, const T* a, int64_t n) {
+    v.assign(a, a + (n > 0 && a ? n : 0));
+  }
+  void copy_from(const abx_problem& q) {
+    p = q;
+    take(eb, q.energy_bounds, q.settings.ngroups + 1);
+    take(mg, q.mg_data, q.n_mg_data);
+    take(teb, q.tally_ebounds, q.n_tally_ebounds);
+    take(surf, q.surfaces, q.n_surfaces);
+    take(cells, q.cells, q.n_cells);
+    take(rpn, q.rpn, q.n_rpn);
+    take(lists, q.cell_lists, q.n_cell_lists);
+    take(lat, q.lattice_elems, q.n_lattice_elems);
+    take(univ, q.universes, q.n_universes);
+    take(mats, q.materials, q.n_materials);
+    take(tallies, q.tallies, q.n_tallies);
+    take(src, q.sources, q.n_sources);
+    p.energy_bounds = eb.data();
+    p.mg_data = mg.data();
+    p.tally_ebounds = teb.data();
+    p.surfaces = surf.data();
+    p.cells = cells.data();
+    p.rpn = rpn.data();
+    p.cell_lists = lists.data();
+    p.lattice_elems = lat.data();
+    p.universes = univ.data();
+    p.materials = mats.data();
+    p.tallies = tallies.data();
+    p.sources = src.data();
+  }
+  uint64_t tally_bins() const {
+    uint64_t n = 0;
+    for (const abx_mesh_tally& t : tallies)
+      n += (uint64_t)std::max(0, t.n_ebounds - 1) * (uint64_t)std::max(0, t.shape[0]) *
+           (uint64_t)std::max(0, t.shape[1]) * (uint64_t)std::max(0, t.shape[2]);
+    return n;
+  }
+  // Device bytes while the request runs: three FP64 arrays per tally bin,
+  // the double and float banks and sort counters per history, and the tables
+  // (four copies of the cross-section data covers the derived CDFs, angle
+  // tables and FP32 mirrors).
+  uint64_t footprint() const {
+    const uint64_t hist = (uint64_t)(p.settings.nparticles > 0 ? p.settings.nparticles : 0);
+    return 24 * tally_bins() + 176 * hist + 32 * (uint64_t)mg.size() +
+           16 * (uint64_t)(surf.size() + cells.size() + rpn.size() + univ.size() + lat.size()) + (64u << 10);
+  }
+};
+
+struct Request {
+  uint64_t id = 0, tag = 0;
+  std::unique_ptr<ProblemCopy> prob;
+  uint64_t footprint = 0;
+  Clock::time_point t_submit;
+};
+
+struct Done {
+  abx_request_result r{};
+  std::vector<double> avg, var;
+};
+
+}  // namespace
+
+struct abx_server {
+  abx_server_options opt{};
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Request> queue;
+  std::deque<uint64_t> ready;                  // finished, not yet polled
+  std::unordered_map<uint64_t, Done> results;  // finished, not yet released
+  uint64_t next_id = 1;
+  bool stop = false;
+  abx_server_stats stats{};
+  std::thread worker;
+  int round = 0;
+
+  void run_round(std::vector<Request>& reqs, Clock::time_point t_start);
+  void finish(Request& q, Done&& d, double queue_ms);
+  void loop();
+};
+
+void abx_server::finish(Request& q, Done&& d, double queue_ms) {
+  d.r.request_id = q.id;
+  d.r.tag = q.tag;
+  d.r.queue_ms = queue_ms;
+  std::lock_guard<std::mutex> g(mu);
+  d.r.latency_ms = ms_between(q.t_submit, Clock::now());
+  stats.completed++;
+  if (d.r.status != ABX_OK) stats.failed++;
+  ready.push_back(q.id);
+  results.emplace(q.id, std::move(d));
+  cv_done.notify_all();
+}
+
+void abx_server::run_round(std::vector<Request>& reqs, Clock::time_point t_start) {
+  const int n = (int)reqs.size();
+  std::vector<abx_problem> arr((size_t)n);
+  for (int i = 0; i < n; i++) arr[(size_t)i] = reqs[(size_t)i].prob->p;
+  abx_ctx* ctx = nullptr;
+  int rc = abx_create_batch(arr.data(), n, opt.device, &ctx);
+  if (rc != ABX_OK && n > 1) {
+    // one of them is malformed: run each alone so the others still complete
+    for (int i = 0; i < n; i++) {
+      std::vector<Request> one;
+      one.push_back(std::move(reqs[(size_t)i]));
+      run_round(one, t_start);
+    }
+    return;
+  }
+  std::vector<abx_problem_result> res((size_t)n);
+  abx_run_stats st{};
+  if (rc == ABX_OK) rc = abx_run_fixed_source_batch(ctx, opt.nbatches, res.data(), &st);
+  std::vector<double> avg, var;
+  if (rc == ABX_OK && opt.keep_tallies) {
+    size_t nb = 0;
+    rc = abx_tally_read_all(ctx, nullptr, nullptr, 0, &nb);
+    if (rc == ABX_OK) {
+      avg.resize(nb);
+      var.resize(nb);
+      rc = abx_tally_read_all(ctx, avg.data(), var.data(), nb, &nb);
+    }
+  }
+  if (ctx) abx_destroy(ctx);
+  {
+    std::lock_guard<std::mutex> g(mu);
+    stats.rounds++;
+    if (rc == ABX_OK) {
+      stats.collisions += st.collisions;
+      stats.flights += st.flights;
+      stats.histories += st.histories;
+      stats.transport_ms += st.transport_ms;
+    }
+  }
+  uint64_t bin0 = 0;
+  const int this_round = round;
+  for (int i = 0; i < n; i++) {
+    Request& q = reqs[(size_t)i];
+    Done d;
+    d.r.status = rc;
+    d.r.round = this_round;
+    d.r.round_problems = n;
+    d.r.n_tallies = q.prob->p.n_tallies;
+    d.r.n_tally_bins = q.prob->tally_bins();
+    if (rc == ABX_OK) {
+      d.r.result = res[(size_t)i];
+      if (opt.keep_tallies) {
+        d.avg.assign(avg.begin() + (long)bin0, avg.begin() + (long)(bin0 + d.r.n_tally_bins));
+        d.var.assign(var.begin() + (long)bin0, var.begin() + (long)(bin0 + d.r.n_tally_bins));
+      }
+    }
+    bin0 += d.r.n_tally_bins;
+    finish(q, std::move(d), ms_between(q.t_submit, t_start));
+  }
+}
+
+void abx_server::loop() {
+  for (;;) {
+    std::vector<Request> reqs;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+      if (stop) break;
+      uint64_t used = 0;
+      while (!queue.empty()) {
+        const Request& h = queue.front();
+        if (!reqs.empty() && used + h.footprint > opt.hbm_budget_bytes) break;
+        if (opt.max_round_problems > 0 && (int)reqs.size() >= opt.max_round_problems) break;
+        used += h.footprint;
+        reqs.push_back(std::move(queue.front()));
+        queue.pop_front();
+      }
+      round++;
+    }
+    const Clock::time_point t0 = Clock::now();
+    run_round(reqs, t0);
+    std::lock_guard<std::mutex> g(mu);
+    stats.busy_ms += ms_between(t0, Clock::now());
+  }
+  // cancel what is still queued
+  std::lock_guard<std::mutex> g(mu);
+  while (!queue.empty()) {
+    Request q = std::move(queue.front());
+    queue.pop_front();
+    Done d;
+    d.r.request_id = q.id;
+    d.r.tag = q.tag;
+    d.r.status = ABX_ERR_CANCELLED;
+    d.r.latency_ms = ms_between(q.t_submit, Clock::now());
+    stats.completed++;
+    stats.failed++;
+    ready.push_back(q.id);
+    results.emplace(q.id, std::move(d));
+  }
+  cv_done.notify_all();
+}
+
+extern "C" int abx_server_create(const abx_server_options* options, abx_server** out) {
+  if (!options || !out) return srv_fail(ABX_ERR_INVALID, "bad arguments");
+  *out = nullptr;
+  if (options->nbatches < 1) return srv_fail(ABX_ERR_INVALID, "nbatches must be >= 1");
+  if (options->precision != ABX_PREC_FP64 && options->precision != ABX_PREC_MIXED)
+    return srv_fail(ABX_ERR_INVALID, "precision %d", options->precision);
+  if (options->tracking != ABX_TRACK_DELTA && options->tracking != ABX_TRACK_SURFACE)
+    return srv_fail(ABX_ERR_INVALID, "tracking %d", options->tracking);
+  abx_server* s = new abx_server();
+  s->opt = *options;
+  if (!s->opt.hbm_budget_bytes) s->opt.hbm_budget_bytes = 150ull * 1000 * 1000 * 1000;
+  s->worker = std::thread([s] { s->loop(); });
+  *out = s;
+  return ABX_OK;
+}
+
+extern "C" int abx_server_destroy(abx_server* s) {
+  if (!s) return ABX_OK;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  delete s;
+  return ABX_OK;
+}
+
+extern "C" int abx_server_submit(abx_server* s, const abx_problem* problem, uint64_t tag, uint64_t* request_id) {
+  if (!s || !problem) return srv_fail(ABX_ERR_INVALID, "bad arguments");
+  const abx_settings& st = problem->settings;
+  if (st.mode != ABX_MODE_FIXED_SOURCE) return srv_fail(ABX_ERR_UNSUPPORTED, "the request loop runs fixed-source problems");
+  if (st.precision != s->opt.precision || st.tracking != s->opt.tracking)
+    return srv_fail(ABX_ERR_UNSUPPORTED, "request precision/tracking differ from the server's");
+  if (st.ngroups < 1 || !problem->energy_bounds || !(st.nparticles >= 1))
+    return srv_fail(ABX_ERR_INVALID, "malformed problem");
+  Request q;
+  q.prob.reset(new ProblemCopy());
+  q.prob->copy_from(*problem);
+  q.footprint = q.prob->footprint();
+  q.tag = tag;
+  if (q.footprint > s->opt.hbm_budget_bytes)
+    return srv_fail(ABX_ERR_BUDGET, "request needs ~%llu bytes, budget %llu", (unsigned long long)q.footprint,
+                    (unsigned long long)s->opt.hbm_budget_bytes);
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->stop) return srv_fail(ABX_ERR_CANCELLED, "server is stopping");
+    q.id = s->next_id++;
+    q.t_submit = Clock::now();
+    if (request_id) *request_id = q.id;
+    s->stats.submitted++;
+    s->queue.push_back(std::move(q));
+  }
+  s->cv_work.notify_one();
+  return ABX_OK;
+}
+
+extern "C" int abx_server_poll(abx_server* s, abx_request_result* out, int capacity, int* n_out, int timeout_ms) {
+  if (!s || !n_out || (capacity > 0 && !out)) return srv_fail(ABX_ERR_INVALID, "bad arguments");
+  *n_out = 0;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto have = [&] { return !s->ready.empty(); };
+  if (!have() && timeout_ms != 0) {
+    if (timeout_ms < 0) {
+      s->cv_done.wait(lk, [&] { return have() || (s->stop && s->queue.empty()); });
+    } else {
+      s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), have);
+    }
+  }
+  int k = 0;
+  while (k < capacity && !s->ready.empty()) {
+    const uint64_t id = s->ready.front();
+    s->ready.pop_front();
+    auto it = s->results.find(id);
+    if (it == s->results.end()) continue;
+    out[k++] = it->second.r;
+    if (!s->opt.keep_tallies) s->results.erase(it);  // nothing left to read
+  }
+  *n_out = k;
+  return ABX_OK;
+}
+
+extern "C" int abx_server_tally(abx_server* s, uint64_t request_id, double* avg, double* var, size_t capacity) {
+  if (!s) return srv_fail(ABX_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  auto it = s->results.find(request_id);
+  if (it == s->results.end()) return srv_fail(ABX_ERR_INVALID, "request %llu has no result", (unsigned long long)request_id);
+  const Done& d = it->second;
+  if (!s->opt.keep_tallies) return srv_fail(ABX_ERR_UNSUPPORTED, "server was created without keep_tallies");
+  if (capacity < d.avg.size()) return srv_fail(ABX_ERR_CAPACITY, "%zu bins, capacity %zu", d.avg.size(), capacity);
+  if (avg && !d.avg.empty()) memcpy(avg, d.avg.data(), d.avg.size() * sizeof(double));
+  if (var && !d.var.empty()) memcpy(var, d.var.data(), d.var.size() * sizeof(double));
+  return ABX_OK;
+}
+
+extern "C" int abx_server_release(abx_server* s, uint64_t request_id) {
+  if (!s) return srv_fail(ABX_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  s->results.erase(request_id);
+  return ABX_OK;
+}
+
+extern "C" int abx_server_get_stats(abx_server* s, abx_server_stats* out) {
+  if (!s || !out) return srv_fail(ABX_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  *out = s->stats;
+  return ABX_OK;
+}

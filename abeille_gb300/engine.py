@@ -155,6 +155,60 @@ class BatchEngine(Engine):
         return rows, stats_dict(st)
 
 
+class Server:
+    """The request loop: fixed-source problems submitted one at a time are
+    batched by a native scheduler thread under an HBM admission budget."""
+
+    def __init__(self, device=0, precision="mixed", tracking="delta-tracking", nbatches=10, hbm_budget_bytes=0,
+                 max_round_problems=0, keep_tallies=True):
+        self.lib = abi.load()
+        o = abi.ServerOptions(device, abi.PRECISION[precision], abi.TRACKING[tracking], nbatches, hbm_budget_bytes,
+                              max_round_problems, int(bool(keep_tallies)))
+        self.srv = C.c_void_p()
+        abi.check(self.lib.abx_server_create(C.byref(o), C.byref(self.srv)), self.lib)
+
+    def submit(self, built, tag=0):
+        rid = C.c_uint64()
+        abi.check(self.lib.abx_server_submit(self.srv, built.ptr, tag, C.byref(rid)), self.lib)
+        return rid.value
+
+    def poll(self, capacity=256, timeout_ms=0):
+        out = (abi.RequestResult * capacity)()
+        n = C.c_int()
+        abi.check(self.lib.abx_server_poll(self.srv, out, capacity, C.byref(n), timeout_ms), self.lib)
+        rows = []
+        for r in out[: n.value]:
+            d = {f: getattr(r, f) for f, _ in abi.RequestResult._fields_ if f != "result"}
+            d.update({f: getattr(r.result, f) for f, _ in abi.ProblemResult._fields_})
+            rows.append(d)
+        return rows
+
+    def tally(self, request_id, nbins):
+        avg, var = np.zeros(nbins), np.zeros(nbins)
+        abi.check(self.lib.abx_server_tally(self.srv, request_id, avg.ctypes.data, var.ctypes.data, nbins),
+                  self.lib)
+        return avg, var
+
+    def release(self, request_id):
+        abi.check(self.lib.abx_server_release(self.srv, request_id), self.lib)
+
+    def stats(self):
+        st = abi.ServerStats()
+        abi.check(self.lib.abx_server_get_stats(self.srv, C.byref(st)), self.lib)
+        return {f: getattr(st, f) for f, _ in abi.ServerStats._fields_}
+
+    def close(self):
+        if self.srv:
+            self.lib.abx_server_destroy(self.srv)
+            self.srv = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class _GpuTracker:
     """Transporter::transport on the GPU: consumes the bank, returns the
     fission bank in BankedParticle::operator< order."""

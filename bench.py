@@ -191,12 +191,17 @@ def main():
     ap.add_argument("--tracking", default=None, choices=["delta-tracking", "surface-tracking"])
     ap.add_argument("--problems", type=int, default=4096, help="config 3: problems in the batch")
     ap.add_argument("--per-problem-sample", type=int, default=128,
-                    help="config 3: problems timed one launch per problem")
+                    help="config 3/4: problems timed one launch per problem")
+    ap.add_argument("--rates", default="200,1000,5000", help="config 4: Poisson arrival rates, requests/s")
+    ap.add_argument("--duration", type=float, default=3.0, help="config 4: seconds of arrivals per rate")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="config 4: HBM admission budget")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.config == 3:
         return bench_batch(args)
+    if args.config == 4:
+        return bench_server(args)
 
     import __graft_entry__
     __graft_entry__.build()
@@ -292,7 +297,7 @@ def bench_batch(args):
     import __graft_entry__
     __graft_entry__.build()
     import numpy as np
-    from abeille_gb300 import BatchEngine, Engine, decks
+    from abeille_gb300 import BatchEngine, decks
 
     rank, world, local, dist = dist_setup(args.gpus)
     nb = args.steps
@@ -344,22 +349,7 @@ def bench_batch(args):
 
     # one problem per launch, on an evenly spaced sample of the same problems
     idx = np.linspace(0, args.problems - 1, min(args.per_problem_sample, args.problems)).astype(int)
-    per = {}
-    for prec in sorted({args.precision, "fp64"}):
-        c_sum, wall, dev = 0, 0.0, 0.0
-        for i in idx:
-            b = decks.fixed_source_problem(int(i), seed=3, precision=prec, batches=nb)
-            if args.tracking:
-                b.tracking = args.tracking
-            e = Engine(b.build(precision=prec), local)
-            ta = time.perf_counter()
-            s1 = e.run_fixed_source(nb, b.nparticles)
-            wall += time.perf_counter() - ta
-            dev += s1["transport_ms"] / 1e3
-            c_sum += s1["collisions"]
-            e.close()
-        per[prec] = {"value": c_sum / wall, "transport_only_value": c_sum / dev, "unit": "collisions/s",
-                     "problems": len(idx), "precision": prec}
+    per = _per_problem_launch(idx, nb, sorted({args.precision, "fp64"}), local, args.tracking)
     b = BYTES[args.precision]
     alg = flights * b["flight"] + coll * b["collision"]
     peak, src = peaks()
@@ -401,6 +391,144 @@ def bench_batch(args):
         "detail": {"collisions": coll, "flights": flights, "transport_ms": tr_ms, "create_s": t_create,
                    "run_wall_s": t_run, "tally_read_s": t_read,
                    "lost": int(sum(r["lost"] for r in rows))},
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+    return 0
+
+
+def _per_problem_launch(idx, nb, precisions, device, tracking=None):
+    """Collisions/s of problems run one per context and launch (FixedSource
+    loop each), wall time around the run."""
+    from abeille_gb300 import Engine, decks
+    per = {}
+    for prec in precisions:
+        c_sum, wall, dev = 0, 0.0, 0.0
+        for i in idx:
+            b = decks.fixed_source_problem(int(i), seed=3, precision=prec, batches=nb)
+            if tracking:
+                b.tracking = tracking
+            e = Engine(b.build(precision=prec), device)
+            ta = time.perf_counter()
+            s1 = e.run_fixed_source(nb, b.nparticles)
+            wall += time.perf_counter() - ta
+            dev += s1["transport_ms"] / 1e3
+            c_sum += s1["collisions"]
+            e.close()
+        per[prec] = {"value": c_sum / wall, "transport_only_value": c_sum / dev, "unit": "collisions/s",
+                     "problems": len(idx), "precision": prec}
+    return per
+
+
+def bench_server(args):
+    """Config 4: config-3 problems arriving as a Poisson stream at each rate of
+    `--rates` for `--duration` s, served by the request loop (mixed
+    precision); latency percentiles per rate, aggregate collisions/s, the
+    FP64 one-problem-per-launch rate, and the leakage z-scores of the served
+    results against FP64 runs of the same problems."""
+    import threading
+
+    import __graft_entry__
+    __graft_entry__.build()
+    import numpy as np
+    from abeille_gb300 import BatchEngine, Server, abi, decks
+
+    rank, world, local, dist = dist_setup(args.gpus)
+    nb = 10
+    npool = min(args.problems, 4096)
+    builders = [decks.fixed_source_problem(i, seed=3 + rank, precision=args.precision, batches=nb)
+                for i in range(npool)]
+    builts = [b.build(precision=args.precision) for b in builders]
+    rates = [float(x) for x in args.rates.split(",") if x]
+    rng = np.random.default_rng(11 + rank)
+
+    def serve(rate, duration, record):
+        srv = Server(device=local, precision=args.precision, nbatches=nb,
+                     hbm_budget_bytes=int(args.budget_gb * 1e9), keep_tallies=False)
+        done, lock = {}, threading.Lock()
+        stop = threading.Event()
+
+        def poller():
+            while not (stop.is_set() and len(done) >= n_sub[0]):
+                for r in srv.poll(512, 50):
+                    with lock:
+                        done[r["request_id"]] = (r, time.perf_counter())
+        n_sub = [10 ** 9]
+        th = threading.Thread(target=poller, daemon=True)
+        th.start()
+        st0 = srv.stats()
+        t0 = time.perf_counter()
+        t_next, i, sub = t0, 0, {}
+        while True:
+            t_next += rng.exponential(1.0 / rate)
+            if t_next - t0 > duration:
+                break
+            while time.perf_counter() < t_next:
+                pass
+            sub[srv.submit(builts[i % npool], tag=i % npool)] = time.perf_counter()
+            i += 1
+        n_sub[0] = len(sub)
+        stop.set()
+        th.join(timeout=600)
+        st1 = srv.stats()
+        srv.close()
+        lat = np.array([done[k][0]["latency_ms"] for k in sub if k in done])
+        t_end = max(v[1] for v in done.values()) if done else time.perf_counter()
+        coll = st1["collisions"] - st0["collisions"]
+        rows = [done[k][0] for k in sub if k in done]
+        out = {"rate": rate, "requests": len(sub), "completed": len(lat),
+               "failed": int(sum(1 for r in rows if r["status"] != 0)),
+               "p50_ms": float(np.percentile(lat, 50)), "p95_ms": float(np.percentile(lat, 95)),
+               "p99_ms": float(np.percentile(lat, 99)), "collisions_per_s": coll / (t_end - t0),
+               "rounds": st1["rounds"] - st0["rounds"], "busy_ms": st1["busy_ms"] - st0["busy_ms"],
+               "transport_ms": st1["transport_ms"] - st0["transport_ms"], "collisions": coll}
+        if record is not None:
+            record.extend(rows)
+        return out
+
+    serve(rates[0], 0.3, None)  # warm-up
+    if dist:
+        dist.barrier()
+    sweep, served = [], []
+    with Clocks(local) as clk:
+        for rate in rates:
+            sweep.append(serve(rate, args.duration, served if rate == rates[-1] else None))
+    head = sweep[-1]
+    if rank != 0:
+        if dist:
+            dist.barrier()
+        return 0
+    # z-scores of the served (mixed) leakage against FP64 runs of the same problems
+    uniq = {}
+    for r in served:
+        uniq.setdefault(r["tag"], r)
+    tags = sorted(uniq)[:512]
+    f64 = [decks.fixed_source_problem(t, seed=3 + rank, precision="fp64", batches=nb).build(precision="fp64")
+           for t in tags]
+    be = BatchEngine(f64, local)
+    rows64, _ = be.run(nb)
+    be.close()
+    z = np.array([(uniq[t]["leak_avg"] - r64["leak_avg"]) / np.hypot(uniq[t]["leak_std"], r64["leak_std"])
+                  for t, r64 in zip(tags, rows64) if np.hypot(uniq[t]["leak_std"], r64["leak_std"]) > 0])
+    idx = np.linspace(0, npool - 1, min(args.per_problem_sample, npool)).astype(int)
+    per = _per_problem_launch(idx, nb, ["fp64"], local)
+    line = {
+        "metric": "collisions/s", "value": head["collisions_per_s"], "unit": "collisions/s", "n_gpus": world,
+        "steps": len(rates), "warmup": 1, "ms_per_step": 1e3 * args.duration, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-track/f64-tally" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": "config4", "arrivals": "poisson", "rates": rates, "duration_s": args.duration,
+                   "problem_pool": npool, "batches": nb, "hbm_budget_gb": args.budget_gb,
+                   "precision": args.precision, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 at the high rates (rounds of thousands of problems)"},
+        "latency": sweep,
+        "per_problem_launch": per,
+        "zscore_vs_fp64": {"problems": int(z.size), "frac_abs_z_lt_2": float(np.mean(np.abs(z) < 2)),
+                           "mean_z": float(z.mean())},
+        "e2e": {"value": head["collisions_per_s"], "unit": "collisions/s", "h2d_bytes_per_step": None,
+                "d2h_bytes_per_step": None, "what": "abx_server_submit .. abx_server_poll wall, all requests"},
+        "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
     if dist:

@@ -391,6 +391,69 @@ int abx_create_batch(const abx_problem* problems, int n_problems, int device, ab
 int abx_run_fixed_source_batch(abx_ctx* ctx, int nbatches, abx_problem_result* results,
                                abx_run_stats* stats);
 
+/* Every tally bin of a context in one copy: the bins of tally 0, then tally
+ * 1, ... (the layout of abx_tally_read).  `avg` / `var` (either may be NULL)
+ * hold `capacity` doubles; `n_bins` receives the total. */
+int abx_tally_read_all(abx_ctx* ctx, double* avg, double* var, size_t capacity, size_t* n_bins);
+
+/* ---------------------------------------------------------- request loop */
+/* A serving loop for fixed-source problems (no reference counterpart: the
+ * reference runs one deck per process).  Requests are copied at submission and
+ * queued; a scheduler thread admits queued requests in arrival order while
+ * their estimated device footprint fits the HBM budget, transports them
+ * together as one batch context (abx_create_batch + abx_run_fixed_source_batch),
+ * and hands results back through abx_server_poll.  While one round runs, new
+ * arrivals queue for the next.  Every request's results equal those of its
+ * problem run alone: batch b of a problem always transports the same
+ * histories with the same per-history random streams. */
+typedef struct abx_server abx_server;
+
+typedef struct abx_server_options {
+  int32_t device;
+  int32_t precision;          /* ABX_PREC_*: every request must match       */
+  int32_t tracking;           /* ABX_TRACK_*: every request must match      */
+  int32_t nbatches;           /* FixedSource batches per request (>= 1)     */
+  uint64_t hbm_budget_bytes;  /* admission budget per round; 0: 150 GB      */
+  int32_t max_round_problems; /* 0: no limit                                */
+  int32_t keep_tallies;       /* copy each request's tally bins back        */
+} abx_server_options;
+
+typedef struct abx_request_result {
+  uint64_t request_id;
+  uint64_t tag;               /* the caller's tag from abx_server_submit    */
+  int32_t status;             /* ABX_OK or this request's error             */
+  int32_t round;              /* scheduling round that ran it               */
+  int32_t round_problems;     /* requests in that round                     */
+  int32_t n_tallies;
+  uint64_t n_tally_bins;      /* bins over all its tallies                  */
+  abx_problem_result result;
+  double queue_ms;            /* submission -> start of its round           */
+  double latency_ms;          /* submission -> result available             */
+} abx_request_result;
+
+typedef struct abx_server_stats {
+  uint64_t submitted, completed, failed, rounds;
+  uint64_t collisions, flights, histories;
+  double busy_ms;             /* wall time spent running rounds             */
+  double transport_ms;        /* device time inside transport kernels       */
+} abx_server_stats;
+
+int abx_server_create(const abx_server_options* options, abx_server** out);
+/* Stops admitting, finishes the running round, cancels queued requests and
+ * frees everything. */
+int abx_server_destroy(abx_server* server);
+/* Copies `problem` (fixed-source, matching the server's precision and
+ * tracking) and queues it.  ABX_ERR_BUDGET when it alone exceeds the budget. */
+int abx_server_submit(abx_server* server, const abx_problem* problem, uint64_t tag, uint64_t* request_id);
+/* Moves up to `capacity` finished results into `out`, waiting up to
+ * `timeout_ms` (0: no wait, <0: until one is available) for the first. */
+int abx_server_poll(abx_server* server, abx_request_result* out, int capacity, int* n_out, int timeout_ms);
+/* Tally bins (avg, var; either may be NULL) of a polled request, in its own
+ * tally order; `capacity` doubles each.  Available until released. */
+int abx_server_tally(abx_server* server, uint64_t request_id, double* avg, double* var, size_t capacity);
+int abx_server_release(abx_server* server, uint64_t request_id);
+int abx_server_get_stats(abx_server* server, abx_server_stats* stats);
+
 /* -------------------------------------------------------- diagnostics */
 /* Per-event trace of the first `n_hist` histories of the next abx_transport
  * call (test hook).  Each record: history index, event kind, rng state,

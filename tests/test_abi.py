@@ -34,7 +34,9 @@ def test_struct_layouts_match_c():
                "abx_source": abi.Source, "abx_settings": abi.Settings, "abx_problem": abi.Problem,
                "abx_particle": abi.Particle, "abx_site": abi.Site, "abx_scores": abi.Scores,
                "abx_run_stats": abi.RunStats, "abx_trace_rec": abi.TraceRec,
-               "abx_gen_record": abi.GenRecord, "abx_problem_result": abi.ProblemResult}
+               "abx_gen_record": abi.GenRecord, "abx_problem_result": abi.ProblemResult,
+               "abx_server_options": abi.ServerOptions, "abx_request_result": abi.RequestResult,
+               "abx_server_stats": abi.ServerStats}
     src = '#include <stdio.h>\n#include <stddef.h>\n#include "abeille_gb300.h"\nint main(void){\n'
     for name in structs:
         src += f'printf("%zu\\n", sizeof({name}));\n'
