@@ -159,7 +159,9 @@ class RequestResult(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
                 ("rounds", C.c_uint64), ("collisions", C.c_uint64), ("flights", C.c_uint64),
-                ("histories", C.c_uint64), ("busy_ms", C.c_double), ("transport_ms", C.c_double)]
+                ("histories", C.c_uint64), ("busy_ms", C.c_double), ("transport_ms", C.c_double),
+                ("create_ms", C.c_double), ("run_ms", C.c_double), ("readback_ms", C.c_double),
+                ("destroy_ms", C.c_double)]
 
 
 # every entry point declared in include/abeille_gb300.h, with its argument types

@@ -336,17 +336,28 @@ static int append_problem(Pools& P, const abx_problem* pr) {
     M.iso = 1;
     for (int gi = 0; gi < G; gi++)
       for (int go = 0; go < G; go++) {
-        std::vector<double> a = {0.5};
+        double ac[6] = {0.5, 0., 0., 0., 0., 0.};
+        bool flat = true;
         for (int l = 1; l <= mt.n_legendre; l++) {
           double coeff = legm[((size_t)(l - 1) * G + gi) * G + go];
-          a.resize((size_t)l + 1, 0.);
-          a[(size_t)l] = coeff * (2. * (double)l + 1.) / 2.;
+          ac[l] = coeff * (2. * (double)l + 1.) / 2.;
+          flat = flat && ac[l] == 0.;
         }
+        AngHdr h{(int)P.ang_d.size(), 2};
+        if (flat) {
+          // pdf 1/2 on [-1, 1]: linearize stops at once with mu {-1, 1},
+          // p {1/2, 1/2}, cdf {0, 1}
+          const double iso_tab[6] = {-1., 1., 0.5, 0.5, 0., 1.};
+          P.ang_d.insert(P.ang_d.end(), iso_tab, iso_tab + 6);
+          P.ang_hdr.push_back(h);
+          continue;
+        }
+        const std::vector<double> a(ac, ac + mt.n_legendre + 1);
         std::vector<double> mu, pp, cc;
         if (!linearize(a, mu, pp, cc)) return fail(ABX_ERR_INVALID, "material %u: angle table did not converge", mt.id);
         bool iso = mu.size() == 2 && pp[0] == 0.5 && pp[1] == 0.5 && cc[0] == 0. && cc[1] == 1.;
         if (!iso) M.iso = 0;
-        AngHdr h{(int)P.ang_d.size(), (int)mu.size()};
+        h.n = (int)mu.size();
         P.ang_d.insert(P.ang_d.end(), mu.begin(), mu.end());
         P.ang_d.insert(P.ang_d.end(), pp.begin(), pp.end());
         P.ang_d.insert(P.ang_d.end(), cc.begin(), cc.end());

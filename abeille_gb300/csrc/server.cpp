@@ -160,7 +160,9 @@ void abx_server::run_round(std::vector<Request>& reqs, Clock::time_point t_start
   std::vector<abx_problem> arr((size_t)n);
   for (int i = 0; i < n; i++) arr[(size_t)i] = reqs[(size_t)i].prob->p;
   abx_ctx* ctx = nullptr;
+  const Clock::time_point c0 = Clock::now();
   int rc = abx_create_batch(arr.data(), n, opt.device, &ctx);
+  const Clock::time_point c1 = Clock::now();
   if (rc != ABX_OK && n > 1) {
     // one of them is malformed: run each alone so the others still complete
     for (int i = 0; i < n; i++) {
@@ -173,6 +175,7 @@ void abx_server::run_round(std::vector<Request>& reqs, Clock::time_point t_start
   std::vector<abx_problem_result> res((size_t)n);
   abx_run_stats st{};
   if (rc == ABX_OK) rc = abx_run_fixed_source_batch(ctx, opt.nbatches, res.data(), &st);
+  const Clock::time_point c2 = Clock::now();
   std::vector<double> avg, var;
   if (rc == ABX_OK && opt.keep_tallies) {
     size_t nb = 0;
@@ -183,10 +186,16 @@ void abx_server::run_round(std::vector<Request>& reqs, Clock::time_point t_start
       rc = abx_tally_read_all(ctx, avg.data(), var.data(), nb, &nb);
     }
   }
+  const Clock::time_point c3 = Clock::now();
   if (ctx) abx_destroy(ctx);
+  const Clock::time_point c4 = Clock::now();
   {
     std::lock_guard<std::mutex> g(mu);
     stats.rounds++;
+    stats.create_ms += ms_between(c0, c1);
+    stats.run_ms += ms_between(c1, c2);
+    stats.readback_ms += ms_between(c2, c3);
+    stats.destroy_ms += ms_between(c3, c4);
     if (rc == ABX_OK) {
       stats.collisions += st.collisions;
       stats.flights += st.flights;

@@ -436,6 +436,10 @@ typedef struct abx_server_stats {
   uint64_t collisions, flights, histories;
   double busy_ms;             /* wall time spent running rounds             */
   double transport_ms;        /* device time inside transport kernels       */
+  double create_ms;           /* of busy_ms: batch context creation         */
+  double run_ms;              /*   running the batches                      */
+  double readback_ms;         /*   copying tally bins back                  */
+  double destroy_ms;          /*   freeing the batch context                */
 } abx_server_stats;
 
 int abx_server_create(const abx_server_options* options, abx_server** out);
