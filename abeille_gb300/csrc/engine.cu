@@ -662,7 +662,13 @@ struct abx_context {
   uint64_t* seg_off = nullptr;
   int32_t* seg_prob = nullptr;
   uint64_t* seg_hid0 = nullptr;
-  int seg_batches = 0;
+  // the (problem, batch) layout of the last batch run
+  int vb_nb = 0;
+  uint64_t vb_total = 0;
+  ProbT* vprobs = nullptr;
+  TallyT* vtallies = nullptr;
+  size_t tally_gen_cap = 0;
+  Tables batch_tables{};
 };
 
 static void ctx_free(abx_ctx* c) {
@@ -677,7 +683,7 @@ static void ctx_free(abx_ctx* c) {
   void* ps[] = {c->tally_gen, c->tally_avg, c->tally_var, c->st, c->run, c->gen_rec,
                 c->ent_bins, c->ent_total, c->hist_count, c->offsets, c->block_sums, c->sec,
                 c->aos_in, c->aos_out, c->trace, c->flush, c->pscore, c->pcount, c->prun,
-                c->seg_off, c->seg_prob, c->seg_hid0};
+                c->seg_off, c->seg_prob, c->seg_hid0, c->vprobs, c->vtallies};
   for (void* p : ps)
     if (p) cudaFree(p);
   if (c->st_host) cudaFreeHost(c->st_host);
@@ -898,27 +904,50 @@ __global__ void k_gen_end(DevState* st, RunAcc* run, const ProbT* probs, abx_gen
   }
 }
 
-// Per-problem batch statistics of a batch context: the leakage estimator of
+// Per-problem batch statistics of a batch context.  Batch b of problem p was
+// scored as virtual problem v = p*nb + b; the leakage estimator of
 // Tallies::calc_gen_values / record_generation (src/tallies.cpp:159-203,
-// 268-280) for every problem, then the per-problem sums are cleared.
+// 268-280) is applied to batches 0..nb-1 in order, as the reference's loop
+// over generations does, then the per-batch sums are cleared.
 struct ProbRun {
   double leak_avg, leak_var;
   unsigned long long coll, flights, hist, lost;
 };
 __global__ void k_prob_record(double* ps, unsigned long long* pc, ProbRun* pr, const ProbT* probs, int np,
-                              int batch) {
+                              int nb) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
-    double* s = ps + (size_t)p * ABX_PSCORES;
-    unsigned long long* c = pc + (size_t)p * ABX_PCOUNTS;
-    ProbRun r = pr[p];
-    upd(batch, s[3] / probs[p].nparticles, r.leak_avg, r.leak_var);
-    r.coll += c[0];
-    r.flights += c[1];
-    r.hist += c[2];
-    r.lost += c[3];
+    ProbRun r{};
+    for (int b = 0; b < nb; b++) {
+      double* s = ps + ((size_t)p * nb + b) * ABX_PSCORES;
+      unsigned long long* c = pc + ((size_t)p * nb + b) * ABX_PCOUNTS;
+      upd(b + 1, s[3] / probs[p].nparticles, r.leak_avg, r.leak_var);
+      r.coll += c[0];
+      r.flights += c[1];
+      r.hist += c[2];
+      r.lost += c[3];
+      for (int k = 0; k < ABX_PSCORES; k++) s[k] = 0.;
+      for (int k = 0; k < ABX_PCOUNTS; k++) c[k] = 0ull;
+    }
     pr[p] = r;
-    for (int k = 0; k < ABX_PSCORES; k++) s[k] = 0.;
-    for (int k = 0; k < ABX_PCOUNTS; k++) c[k] = 0ull;
+  }
+}
+
+// MeshTally::record_generation + clear_generation (src/mesh_tally.cpp:121-152)
+// for nb batches scored side by side: bin i of batch b sits at gen[b*n + i];
+// the batches are recorded in order into avg/var (which start from zero).
+__global__ void k_tally_record_batches(double* gen, double* avg, double* var, size_t n, int nb) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double a = 0., v = 0.;
+    for (int b = 0; b < nb; b++) {
+      const double dg = (double)(b + 1);
+      const double val = gen[(size_t)b * n + i];
+      const double old_avg = a;
+      a = old_avg + (val - old_avg) / dg;
+      v = v + (((val - old_avg) * (val - a) - (v)) / dg);
+      gen[(size_t)b * n + i] = 0.;
+    }
+    avg[i] = a;
+    var[i] = v;
   }
 }
 
@@ -1060,7 +1089,7 @@ static int check_state(abx_ctx* c) {
 template <class R> static TransportArgs<R> make_args(abx_ctx* c, const BankT<R>& bank, const SiteT<R>& sites,
                                                      size_t site_cap) {
   TransportArgs<R> A{};
-  A.T = c->D.T;
+  A.T = c->batch_scores ? c->batch_tables : c->D.T;
   A.T.tally_gen = c->tally_gen;
   A.bank = bank;
   A.sites = sites;
@@ -1155,6 +1184,7 @@ static int create_ctx(const abx_problem* problems, int nprob, int device, abx_ct
   size_t nb = (size_t)std::max<int64_t>(c->P.tally_bins, 1);
   if (cudaMalloc(&c->tally_gen, nb * 8) || cudaMalloc(&c->tally_avg, nb * 8) || cudaMalloc(&c->tally_var, nb * 8))
     return bail(fail(ABX_ERR_OOM, "tally allocation failed"));
+  c->tally_gen_cap = nb;
   cudaMemset(c->tally_gen, 0, nb * 8);
   cudaMemset(c->tally_avg, 0, nb * 8);
   cudaMemset(c->tally_var, 0, nb * 8);
@@ -1361,7 +1391,7 @@ static int transport_noalloc_impl(abx_ctx* c, unsigned char* scratch, const abx_
   na_carve<R>(scratch, b, s, counts, offsets, blocks);
   k_bank_from_aos<R><<<grid_for(n), 256, 0, c->stream>>>(bank_dev, n, b);
   TransportArgs<R> A{};
-  A.T = c->D.T;
+  A.T = c->batch_scores ? c->batch_tables : c->D.T;
   A.T.tally_gen = c->tally_gen;
   A.bank = b;
   A.sites = s;
@@ -1783,9 +1813,85 @@ extern "C" int abx_run_fixed_source(abx_ctx* c, int nbatches, uint64_t npart, ab
   return ABX_OK;
 }
 
-// Batch b of every problem of a batch context in one transport launch; the
-// per-batch bookkeeping of FixedSource::run (src/fixed_source.cpp:105-150)
-// for every problem at once.
+// Every batch of every problem of a batch context in one transport launch.
+// Batch b of problem p runs as virtual problem v = p*nb + b: a copy of the
+// problem's settings whose tallies are the b-th copy of the problem's tally
+// bins, so the per-batch bookkeeping of FixedSource::run
+// (src/fixed_source.cpp:105-150) is applied afterwards, batch by batch, for
+// every problem at once.
+static int ensure_virtual(abx_ctx* c, int nb) {
+  const int np = c->nprob;
+  const size_t R = (size_t)c->P.tally_bins;
+  const int RT = (int)c->P.tallies.size();
+  if (c->vb_nb == nb) return ABX_OK;
+  std::vector<ProbT> vp((size_t)np * nb);
+  std::vector<TallyT> vt((size_t)RT * nb);
+  for (int p = 0; p < np; p++)
+    for (int b = 0; b < nb; b++) {
+      ProbT q = c->P.probs[p];
+      q.tally_first = b * RT + q.tally_first;
+      vp[(size_t)p * nb + b] = q;
+    }
+  for (int b = 0; b < nb; b++)
+    for (int t = 0; t < RT; t++) {
+      TallyT u = c->P.tallies[t];
+      u.bin_off += (int64_t)b * (int64_t)R;
+      vt[(size_t)b * RT + t] = u;
+    }
+  if (c->vprobs) cudaFree(c->vprobs);
+  if (c->vtallies) cudaFree(c->vtallies);
+  c->vprobs = nullptr;
+  c->vtallies = nullptr;
+  c->vb_nb = 0;
+  CUDA_TRY(cudaMalloc(&c->vprobs, vp.size() * sizeof(ProbT)));
+  CUDA_TRY(cudaMalloc(&c->vtallies, std::max<size_t>(vt.size(), 1) * sizeof(TallyT)));
+  CUDA_TRY(cudaMemcpy(c->vprobs, vp.data(), vp.size() * sizeof(ProbT), cudaMemcpyHostToDevice));
+  if (!vt.empty()) CUDA_TRY(cudaMemcpy(c->vtallies, vt.data(), vt.size() * sizeof(TallyT), cudaMemcpyHostToDevice));
+  const size_t need = std::max<size_t>(R * (size_t)nb, 1);
+  if (c->tally_gen_cap < need) {
+    if (c->tally_gen) cudaFree(c->tally_gen);
+    c->tally_gen = nullptr;
+    c->tally_gen_cap = 0;
+    CUDA_TRY(cudaMalloc(&c->tally_gen, need * 8));
+    c->tally_gen_cap = need;
+  }
+  const size_t nv = (size_t)np * nb;
+  for (void* q : {(void*)c->pscore, (void*)c->pcount, (void*)c->seg_off, (void*)c->seg_prob, (void*)c->seg_hid0})
+    if (q) cudaFree(q);
+  c->pscore = nullptr;
+  c->pcount = nullptr;
+  c->seg_off = nullptr;
+  c->seg_prob = nullptr;
+  c->seg_hid0 = nullptr;
+  CUDA_TRY(cudaMalloc(&c->pscore, nv * ABX_PSCORES * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&c->pcount, nv * ABX_PCOUNTS * sizeof(unsigned long long)));
+  CUDA_TRY(cudaMalloc(&c->seg_off, (nv + 1) * sizeof(uint64_t)));
+  CUDA_TRY(cudaMalloc(&c->seg_prob, nv * sizeof(int32_t)));
+  CUDA_TRY(cudaMalloc(&c->seg_hid0, nv * sizeof(uint64_t)));
+  if (!c->prun) CUDA_TRY(cudaMalloc(&c->prun, (size_t)np * sizeof(ProbRun)));
+  // segments: virtual problem v = p*nb + b holds histories b*n_p .. (b+1)*n_p-1
+  std::vector<uint64_t> off(nv + 1), hid0(nv);
+  std::vector<int32_t> vid(nv);
+  uint64_t total = 0;
+  for (int p = 0; p < np; p++) {
+    const uint64_t n_p = (uint64_t)c->P.probs[p].nparticles;
+    for (int b = 0; b < nb; b++) {
+      const size_t v = (size_t)p * nb + b;
+      off[v] = total;
+      hid0[v] = (uint64_t)b * n_p;  // src/fixed_source.cpp:152-155
+      vid[v] = (int32_t)v;
+      total += n_p;
+    }
+  }
+  off[nv] = total;
+  CUDA_TRY(cudaMemcpy(c->seg_off, off.data(), off.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(c->seg_prob, vid.data(), vid.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(c->seg_hid0, hid0.data(), hid0.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+  c->vb_total = total;
+  c->vb_nb = nb;
+  return ABX_OK;
+}
+
 extern "C" int abx_run_fixed_source_batch(abx_ctx* c, int nbatches, abx_problem_result* results,
                                           abx_run_stats* stats) {
   if (!c || nbatches <= 0) return fail(ABX_ERR_INVALID, "bad arguments");
@@ -1793,101 +1899,71 @@ extern "C" int abx_run_fixed_source_batch(abx_ctx* c, int nbatches, abx_problem_
   cudaSetDevice(c->device);
   const bool mixed = mixed_of(c);
   const int np = c->nprob;
-  std::vector<uint64_t> off((size_t)np + 1);
-  std::vector<int32_t> pid((size_t)np);
   uint64_t total = 0;
   for (int p = 0; p < np; p++) {
-    off[p] = total;
-    pid[p] = p;
-    total += (uint64_t)c->P.probs[p].nparticles;
-  }
-  off[np] = total;
-  if (total == 0 || total > 0xffffffffull) return fail(ABX_ERR_CAPACITY, "%llu histories per batch", (unsigned long long)total);
-  for (int p = 0; p < np; p++) {
     if (c->P.probs[p].src_count <= 0) return fail(ABX_ERR_INVALID, "problem %d has no sources", p);
+    total += (uint64_t)c->P.probs[p].nparticles * (uint64_t)nbatches;
   }
+  if (total == 0 || total > 0xffffffffull)
+    return fail(ABX_ERR_CAPACITY, "%llu histories in one launch", (unsigned long long)total);
   int rc;
+  if ((rc = ensure_virtual(c, nbatches)) != ABX_OK) return rc;
   if ((rc = ensure_banks(c, total, mixed, true)) != ABX_OK) return rc;
   if ((rc = ensure_sites(c, 1, mixed)) != ABX_OK) return rc;
   if ((rc = ensure_sec(c, mixed)) != ABX_OK) return rc;
-  if ((rc = ensure_records(c, nbatches)) != ABX_OK) return rc;
-  if (!c->pscore) {
-    CUDA_TRY(cudaMalloc(&c->pscore, (size_t)np * ABX_PSCORES * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&c->pcount, (size_t)np * ABX_PCOUNTS * sizeof(unsigned long long)));
-    CUDA_TRY(cudaMalloc(&c->prun, (size_t)np * sizeof(ProbRun)));
-    CUDA_TRY(cudaMalloc(&c->seg_off, ((size_t)np + 1) * sizeof(uint64_t)));
-    CUDA_TRY(cudaMalloc(&c->seg_prob, (size_t)np * sizeof(int32_t)));
-  }
-  if (c->seg_batches < nbatches) {
-    if (c->seg_hid0) cudaFree(c->seg_hid0);
-    c->seg_hid0 = nullptr;
-    CUDA_TRY(cudaMalloc(&c->seg_hid0, (size_t)nbatches * np * sizeof(uint64_t)));
-    c->seg_batches = nbatches;
-  }
-  // first history id of batch b of problem p: b * n_p (src/fixed_source.cpp:152-155)
-  std::vector<uint64_t> hid0((size_t)nbatches * np);
-  for (int b = 0; b < nbatches; b++)
-    for (int p = 0; p < np; p++) hid0[(size_t)b * np + p] = (uint64_t)b * (off[p + 1] - off[p]);
-  CUDA_TRY(cudaMemcpyAsync(c->seg_off, off.data(), off.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(c->seg_prob, pid.data(), pid.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(c->seg_hid0, hid0.data(), hid0.size() * sizeof(uint64_t), cudaMemcpyHostToDevice,
-                           c->stream));
+  if ((rc = ensure_records(c, 1)) != ABX_OK) return rc;
+  const size_t nv = (size_t)np * nbatches;
+  const size_t R = (size_t)c->P.tally_bins;
   CUDA_TRY(cudaMemsetAsync(c->st, 0, sizeof(DevState), c->stream));
   CUDA_TRY(cudaMemsetAsync(c->run, 0, sizeof(RunAcc), c->stream));
-  CUDA_TRY(cudaMemsetAsync(c->pscore, 0, (size_t)np * ABX_PSCORES * sizeof(double), c->stream));
-  CUDA_TRY(cudaMemsetAsync(c->pcount, 0, (size_t)np * ABX_PCOUNTS * sizeof(unsigned long long), c->stream));
-  CUDA_TRY(cudaMemsetAsync(c->prun, 0, (size_t)np * sizeof(ProbRun), c->stream));
-  zero_d(c->tally_gen, (size_t)c->P.tally_bins, c->stream);
-  zero_d(c->tally_avg, (size_t)c->P.tally_bins, c->stream);
-  zero_d(c->tally_var, (size_t)c->P.tally_bins, c->stream);
+  CUDA_TRY(cudaMemsetAsync(c->pscore, 0, nv * ABX_PSCORES * sizeof(double), c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->pcount, 0, nv * ABX_PCOUNTS * sizeof(unsigned long long), c->stream));
+  zero_d(c->tally_gen, R * nbatches, c->stream);
   c->tally_g = 0;
-  std::vector<cudaEvent_t> evs(4 * (size_t)nbatches);
-  for (auto& e : evs) cudaEventCreate(&e);
+  Tables TV = c->D.T;
+  TV.probs = c->vprobs;
+  TV.tallies = c->vtallies;
+  TV.nprob = (int)nv;
+  cudaEvent_t ev[4];
+  for (auto& e : ev) cudaEventCreate(&e);
+  cudaEventRecord(ev[0], c->stream);
+  SourceArgs S{};
+  S.T = TV;
+  S.n = total;
+  BankT<double>& b0 = c->bd[0].b;
+  S.x = b0.x; S.y = b0.y; S.z = b0.z; S.ux = b0.ux; S.uy = b0.uy; S.uz = b0.uz; S.E = b0.E; S.w = b0.w;
+  S.w2 = b0.w2; S.rng = b0.rng; S.hid = b0.hid; S.fam = b0.fam; S.probv = b0.prob; S.out_off = 0; S.st = c->st;
+  S.seg_off = c->seg_off;
+  S.seg_prob = c->seg_prob;
+  S.seg_hid0 = c->seg_hid0;
+  S.nseg = (int)nv;
+  launch_sources(S, c->stream);
+  if (mixed) k_bank_d2f<<<grid_for(total), 256, 0, c->stream>>>(b0, c->bf[0].b, 0, total);
+  k_step_begin<<<1, 1, 0, c->stream>>>(c->st, total, 1.0, 1, 0);
+  cudaEventRecord(ev[1], c->stream);
+  c->batch_tables = TV;
   c->batch_scores = true;
-  for (int b = 0; b < nbatches; b++) {
-    cudaEventRecord(evs[4 * b], c->stream);
-    SourceArgs S{};
-    S.T = c->D.T;
-    S.n = total;
-    BankT<double>& b0 = c->bd[0].b;
-    S.x = b0.x; S.y = b0.y; S.z = b0.z; S.ux = b0.ux; S.uy = b0.uy; S.uz = b0.uz; S.E = b0.E; S.w = b0.w;
-    S.w2 = b0.w2; S.rng = b0.rng; S.hid = b0.hid; S.fam = b0.fam; S.probv = b0.prob; S.out_off = 0; S.st = c->st;
-    S.seg_off = c->seg_off;
-    S.seg_prob = c->seg_prob;
-    S.seg_hid0 = c->seg_hid0 + (size_t)b * np;
-    S.nseg = np;
-    launch_sources(S, c->stream);
-    if (mixed) k_bank_d2f<<<grid_for(total), 256, 0, c->stream>>>(b0, c->bf[0].b, 0, total);
-    k_step_begin<<<1, 1, 0, c->stream>>>(c->st, total, 1.0, 1, 0);
-    cudaEventRecord(evs[4 * b + 1], c->stream);
-    if ((rc = launch_transport(c, mixed, 0, 0)) != ABX_OK) break;
-    cudaEventRecord(evs[4 * b + 2], c->stream);
-    if (c->P.tally_bins)
-      k_tally_record<<<grid_for((size_t)c->P.tally_bins), 256, 0, c->stream>>>(
-          c->tally_gen, c->tally_avg, c->tally_var, (size_t)c->P.tally_bins, 1.0, 1, (double)(b + 1));
+  rc = launch_transport(c, mixed, 0, 0);
+  c->batch_scores = false;
+  cudaEventRecord(ev[2], c->stream);
+  if (rc == ABX_OK) {
+    if (R)
+      k_tally_record_batches<<<grid_for(R), 256, 0, c->stream>>>(c->tally_gen, c->tally_avg, c->tally_var, R,
+                                                                  nbatches);
     k_prob_record<<<(np + 255) / 256, 256, 0, c->stream>>>(c->pscore, c->pcount, (ProbRun*)c->prun, c->D.T.probs,
-                                                           np, b + 1);
+                                                           np, nbatches);
     k_gen_end<<<1, 1024, 0, c->stream>>>(c->st, c->run, c->D.T.probs, c->gen_rec, c->hist_cap, c->ent_bins,
                                          nullptr, 0, total, 0, 0);
-    cudaEventRecord(evs[4 * b + 3], c->stream);
-    if (cudaGetLastError() != cudaSuccess) {
-      rc = fail(ABX_ERR_CUDA, "launch failed");
-      break;
-    }
-    if ((b & 7) == 7 || b == nbatches - 1)
-      if ((rc = check_state(c)) != ABX_OK) break;
+    cudaEventRecord(ev[3], c->stream);
+    if (cudaGetLastError() != cudaSuccess) rc = fail(ABX_ERR_CUDA, "launch failed");
   }
-  c->batch_scores = false;
-  if (rc == ABX_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = fail(ABX_ERR_CUDA, "stream sync failed");
-  double tms = 0., sms = 0.;
-  for (int b = 0; b < nbatches && rc == ABX_OK; b++) {
-    float ms = 0.f, ts = 0.f;
-    cudaEventElapsedTime(&ms, evs[4 * b], evs[4 * b + 3]);
-    cudaEventElapsedTime(&ts, evs[4 * b + 1], evs[4 * b + 2]);
-    sms += ms;
-    tms += ts;
+  if (rc == ABX_OK) rc = check_state(c);
+  float sms = 0.f, tms = 0.f;
+  if (rc == ABX_OK) {
+    cudaEventElapsedTime(&sms, ev[0], ev[3]);
+    cudaEventElapsedTime(&tms, ev[1], ev[2]);
   }
-  for (auto& e : evs) cudaEventDestroy(e);
+  for (auto& e : ev) cudaEventDestroy(e);
   if (rc) return rc;
   c->tally_g = nbatches;
   c->last_ms = tms;
@@ -1911,8 +1987,8 @@ extern "C" int abx_run_fixed_source_batch(abx_ctx* c, int nbatches, abx_problem_
   }
   if (stats) {
     memset(stats, 0, sizeof *stats);
-    stats->generations = ra.gen;
-    stats->active = ra.active;
+    stats->generations = nbatches;
+    stats->active = nbatches;
     stats->collisions = ra.total_coll;
     stats->flights = ra.total_flights;
     stats->histories = ra.total_hist;

@@ -4,9 +4,8 @@
 // queues it with an estimate of its device footprint.  One scheduler thread
 // runs rounds: it admits queued requests in arrival order while the sum of
 // their footprints fits the HBM budget, creates one batch context for them,
-// runs every request's batches (batch b of all admitted problems in one
-// transport launch), copies results and tally bins back, and frees the
-// context.  Requests that arrive during a round wait for the next one, so the
+// runs every batch of every admitted request in one transport launch, copies
+// results and tally bins back, and frees the context.  Requests that arrive during a round wait for the next one, so the
 // rounds size themselves to the arrival rate.
 //
 // A request's results do not depend on its round: batch b of a problem
@@ -99,13 +98,14 @@ struct ProblemCopy {
            (uint64_t)std::max(0, t.shape[1]) * (uint64_t)std::max(0, t.shape[2]);
     return n;
   }
-  // Device bytes while the request runs: three FP64 arrays per tally bin,
-  // the double and float banks and sort counters per history, and the tables
+  // Device bytes while the request runs with `nb` batches: a per-batch FP64
+  // copy of every tally bin plus the average and variance, the double and
+  // float banks and sort counters for all its histories, and the tables
   // (four copies of the cross-section data covers the derived CDFs, angle
   // tables and FP32 mirrors).
-  uint64_t footprint() const {
-    const uint64_t hist = (uint64_t)(p.settings.nparticles > 0 ? p.settings.nparticles : 0);
-    return 24 * tally_bins() + 176 * hist + 32 * (uint64_t)mg.size() +
+  uint64_t footprint(int nb) const {
+    const uint64_t hist = (uint64_t)(p.settings.nparticles > 0 ? p.settings.nparticles : 0) * (uint64_t)nb;
+    return 8 * ((uint64_t)nb + 2) * tally_bins() + 176 * hist + 32 * (uint64_t)mg.size() +
            16 * (uint64_t)(surf.size() + cells.size() + rpn.size() + univ.size() + lat.size()) + (64u << 10);
   }
 };
@@ -305,7 +305,7 @@ extern "C" int abx_server_submit(abx_server* s, const abx_problem* problem, uint
   Request q;
   q.prob.reset(new ProblemCopy());
   q.prob->copy_from(*problem);
-  q.footprint = q.prob->footprint();
+  q.footprint = q.prob->footprint(s->opt.nbatches);
   q.tag = tag;
   if (q.footprint > s->opt.hbm_budget_bytes)
     return srv_fail(ABX_ERR_BUDGET, "request needs ~%llu bytes, budget %llu", (unsigned long long)q.footprint,

@@ -289,39 +289,34 @@ def main():
 
 
 def bench_batch(args):
-    """Config 3: `--problems` independent fixed-source slab problems resident
-    together; one step = batch b of every problem in one transport launch
-    (plus source sampling and the per-problem records).  Beside it, a sample
-    of the same problems run one problem per launch (their own context and
-    FixedSource loop each), in the same precision and in FP64."""
+    """Config 3: `--problems` independent fixed-source slab problems (10
+    batches each) resident together.  One step = one run of every batch of
+    every problem: source sampling, one transport launch over all of them, and
+    the per-batch tally and leakage records.  Beside it, a sample of the same
+    problems run one problem per launch (their own context and FixedSource
+    loop each), in the same precision and in FP64."""
     import __graft_entry__
     __graft_entry__.build()
     import numpy as np
     from abeille_gb300 import BatchEngine, decks
 
     rank, world, local, dist = dist_setup(args.gpus)
-    nb = args.steps
+    nb = 10
     builders = [decks.fixed_source_problem(i, seed=3 + rank, precision=args.precision, batches=nb)
                 for i in range(args.problems)]
     if args.tracking:
         for b in builders:
             b.tracking = args.tracking
     builts = [b.build(precision=args.precision) for b in builders]
-    hist_per_batch = sum(b.nparticles for b in builders)
+    hist_per_step = nb * sum(b.nparticles for b in builders)
 
-    warm = BatchEngine(builts, local)
-    warm.run(max(args.warmup, 1))
-    warm.close()
-    if dist:
-        dist.barrier()
+    # end to end, once: create (host tables + upload) + run + every tally read back
     t0 = time.perf_counter()
     eng = BatchEngine(builts, local)
     t_create = time.perf_counter() - t0
-    with Clocks(local) as clk:
-        t1 = time.perf_counter()
-        rows, st = eng.run(nb)
-        t_run = time.perf_counter() - t1
-    # end to end: create (host tables + upload) + run + every problem's tally read back
+    t1 = time.perf_counter()
+    rows, st_e = eng.run(nb)
+    t_run = time.perf_counter() - t1
     t2 = time.perf_counter()
     d2h = 0
     for r in rows:
@@ -329,9 +324,21 @@ def bench_batch(args):
         d2h += t["avg"].nbytes + t["var"].nbytes + t["gen"].nbytes
     t_read = time.perf_counter() - t2
     e2e_wall = t_create + t_run + t_read
+    e2e_coll = st_e["collisions"]
     h2d = sum(sum(getattr(a, "nbytes", 0) for a in b._keep) for b in builts)
-    coll, flights = st["collisions"], st["flights"]
-    step_ms, tr_ms = st["total_ms"], st["transport_ms"]
+    for _ in range(max(args.warmup - 1, 0)):
+        eng.run(nb)
+    if dist:
+        dist.barrier()
+    coll = flights = 0
+    step_ms = tr_ms = 0.0
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            rows, st = eng.run(nb)
+            coll += st["collisions"]
+            flights += st["flights"]
+            step_ms += st["total_ms"]
+            tr_ms += st["transport_ms"]
     if dist:
         import torch
         t = torch.tensor([step_ms / 1e3, float(coll)], dtype=torch.float64, device=f"cuda:{local}")
@@ -355,7 +362,7 @@ def bench_batch(args):
     peak, src = peaks()
     roof = {"bound": "hbm", "achieved": alg / (tr_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
             "frac": alg / (tr_ms / 1e3) / 1e9 / peak, "traffic": None, "peak_source": src,
-            "kernel": "transport_kernel", "algorithmic_bytes_per_launch": alg / nb}
+            "kernel": "transport_kernel", "algorithmic_bytes_per_launch": alg / args.steps}
     cpu = None
     if world == 1 and not args.no_cpu:
         import oracle
@@ -374,19 +381,19 @@ def bench_batch(args):
                "sample": f"{used} of the problems, {nb} batches each, FP64, one problem at a time"}
     line = {
         "metric": "collisions/s", "value": coll_all / secs, "unit": "collisions/s", "n_gpus": world,
-        "steps": nb, "warmup": args.warmup, "ms_per_step": step_ms / nb, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-track/f64-tally" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": "config3", "problems": args.problems, "histories_per_step": hist_per_batch,
+        "config": {"workload": "config3", "problems": args.problems, "histories_per_step": hist_per_step,
                    "batches": nb, "tracking": builders[0].tracking, "precision": args.precision,
                    "l2": "inputs larger than L2 (bank of all problems' batch, tallies of 4096x8000 bins)",
                    "parallelism": f"replicas{world}"},
         "roofline": roof, "cpu_baseline": cpu,
-        "e2e": {"value": coll_all / e2e_wall, "unit": "collisions/s", "h2d_bytes_per_step": h2d // nb,
-                "d2h_bytes_per_step": d2h // nb,
+        "e2e": {"value": e2e_coll / e2e_wall, "unit": "collisions/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
                 "what": "abx_create_batch + abx_run_fixed_source_batch + every tally read back, wall"},
         "per_problem_launch": per,
-        "gpu_launches": (7 if args.precision == "mixed" else 6) * nb,
+        "gpu_launches": (8 if args.precision == "mixed" else 7) * args.steps,
         "clocks": clk.summary(),
         "detail": {"collisions": coll, "flights": flights, "transport_ms": tr_ms, "create_s": t_create,
                    "run_wall_s": t_run, "tally_read_s": t_read,

@@ -364,9 +364,11 @@ int abx_run_fixed_source(abx_ctx* ctx, int nbatches, uint64_t nparticles,
  * its results are the ones FixedSource::run (src/fixed_source.cpp:81-173)
  * gives for it alone: batch b of problem p transports histories
  * b*n_p .. (b+1)*n_p-1 (n_p = its settings.nparticles), each seeded by
- * skip-ahead on the problem's own stream.  The GPU transports batch b of
- * every problem in one launch.  The reference runs one problem per process;
- * this entry point has no single reference counterpart. */
+ * skip-ahead on the problem's own stream.  The GPU transports every batch of
+ * every problem in one launch, scoring each batch into its own copy of the
+ * problem's tally bins, and then records the batches in order.  The
+ * reference runs one problem per process; this entry point has no single
+ * reference counterpart. */
 typedef struct abx_problem_result {
   double leak_avg;          /* leakage per source particle, mean over batches */
   double leak_std;          /* its standard deviation (of the mean)           */
