@@ -160,8 +160,8 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
                 ("rounds", C.c_uint64), ("collisions", C.c_uint64), ("flights", C.c_uint64),
                 ("histories", C.c_uint64), ("busy_ms", C.c_double), ("transport_ms", C.c_double),
-                ("create_ms", C.c_double), ("run_ms", C.c_double), ("readback_ms", C.c_double),
-                ("destroy_ms", C.c_double)]
+                ("load_ms", C.c_double), ("run_ms", C.c_double), ("readback_ms", C.c_double),
+                ("free_ms", C.c_double)]
 
 
 # every entry point declared in include/abeille_gb300.h, with its argument types
@@ -192,6 +192,7 @@ PROTOTYPES = {
     "abx_set_l2_flush": (C.c_int, [C.c_void_p, C.c_size_t]),
     "abx_create_batch": (C.c_int, [C.POINTER(Problem), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "abx_run_fixed_source_batch": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(ProblemResult), C.POINTER(RunStats)]),
+    "abx_batch_replace": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.c_int]),
     "abx_tally_read_all": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "abx_server_create": (C.c_int, [C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
     "abx_server_destroy": (C.c_int, [C.c_void_p]),

@@ -448,21 +448,38 @@ static int append_problem(Pools& P, const abx_problem* pr) {
 }
 
 // ------------------------------------------------------------ device pools
+// Device copies of the pools.  upload() fills the slots in a fixed order, so
+// a context whose problems are replaced reuses each slot's allocation when it
+// is large enough.
 struct DevPools {
   std::vector<void*> allocs;
+  std::vector<size_t> caps;
+  size_t slot = 0;
   Tables T{};
   template <class X> int up(const std::vector<X>& v, const X** out) {
-    size_t n = std::max<size_t>(v.size(), 1);
-    void* p = nullptr;
-    CUDA_TRY(cudaMalloc(&p, n * sizeof(X)));
-    allocs.push_back(p);
+    const size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(X);
+    if (slot == allocs.size()) {
+      allocs.push_back(nullptr);
+      caps.push_back(0);
+    }
+    if (caps[slot] < bytes) {
+      if (allocs[slot]) cudaFree(allocs[slot]);
+      allocs[slot] = nullptr;
+      caps[slot] = 0;
+      CUDA_TRY(cudaMalloc(&allocs[slot], bytes));
+      caps[slot] = bytes;
+    }
+    void* p = allocs[slot++];
     if (!v.empty()) CUDA_TRY(cudaMemcpy(p, v.data(), v.size() * sizeof(X), cudaMemcpyHostToDevice));
     *out = (const X*)p;
     return ABX_OK;
   }
   void release() {
-    for (void* p : allocs) cudaFree(p);
+    for (void* p : allocs)
+      if (p) cudaFree(p);
     allocs.clear();
+    caps.clear();
+    slot = 0;
   }
 };
 
@@ -474,6 +491,7 @@ template <class X> static std::vector<float> to_f(const std::vector<X>& v) {
 
 static int upload(const Pools& P, DevPools& D) {
   int rc;
+  D.slot = 0;
 #define UP(v, dst)                                  \
   if ((rc = D.up(v, &dst)) != ABX_OK) return rc;
   UP(P.cells, D.T.cells);
@@ -668,6 +686,8 @@ struct abx_context {
   ProbT* vprobs = nullptr;
   TallyT* vtallies = nullptr;
   size_t tally_gen_cap = 0;
+  size_t vcap[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  size_t tally_rv_cap = 0;  // capacity of tally_avg / tally_var, in bins
   Tables batch_tables{};
 };
 
@@ -1185,6 +1205,7 @@ static int create_ctx(const abx_problem* problems, int nprob, int device, abx_ct
   if (cudaMalloc(&c->tally_gen, nb * 8) || cudaMalloc(&c->tally_avg, nb * 8) || cudaMalloc(&c->tally_var, nb * 8))
     return bail(fail(ABX_ERR_OOM, "tally allocation failed"));
   c->tally_gen_cap = nb;
+  c->tally_rv_cap = nb;
   cudaMemset(c->tally_gen, 0, nb * 8);
   cudaMemset(c->tally_avg, 0, nb * 8);
   cudaMemset(c->tally_var, 0, nb * 8);
@@ -1813,6 +1834,54 @@ extern "C" int abx_run_fixed_source(abx_ctx* c, int nbatches, uint64_t npart, ab
   return ABX_OK;
 }
 
+extern "C" int abx_batch_replace(abx_ctx* c, const abx_problem* problems, int n_problems) {
+  if (!c || !problems || n_problems <= 0) return fail(ABX_ERR_INVALID, "bad arguments");
+  for (int i = 0; i < n_problems; i++) {
+    const abx_settings& s = problems[i].settings;
+    if (s.mode != ABX_MODE_FIXED_SOURCE || s.tracking != c->prob0.tracking || s.precision != c->prec)
+      return fail(ABX_ERR_UNSUPPORTED,
+                  "problem %d: a batch holds fixed-source problems of the context's tracking mode and precision", i);
+  }
+  Pools P2;
+  for (int i = 0; i < n_problems; i++) {
+    int rc = append_problem(P2, &problems[i]);
+    if (rc) return rc;  // the context keeps its previous problems
+  }
+  cudaSetDevice(c->device);
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->P = std::move(P2);
+  c->nprob = n_problems;
+  c->prob0 = c->P.probs[0];
+  c->fissile_any = false;
+  for (const MatT& m : c->P.mats) c->fissile_any |= m.fissile != 0;
+  int rc = upload(c->P, c->D);
+  if (rc) return rc;
+  const size_t R = (size_t)std::max<int64_t>(c->P.tally_bins, 1);
+  if (c->tally_rv_cap < R) {
+    cudaFree(c->tally_avg);
+    cudaFree(c->tally_var);
+    c->tally_avg = c->tally_var = nullptr;
+    c->tally_rv_cap = 0;
+    CUDA_TRY(cudaMalloc(&c->tally_avg, R * 8));
+    CUDA_TRY(cudaMalloc(&c->tally_var, R * 8));
+    c->tally_rv_cap = R;
+  }
+  if (c->tally_gen_cap < R) {
+    cudaFree(c->tally_gen);
+    c->tally_gen = nullptr;
+    c->tally_gen_cap = 0;
+    CUDA_TRY(cudaMalloc(&c->tally_gen, R * 8));
+    c->tally_gen_cap = R;
+  }
+  zero_d(c->tally_gen, R, c->stream);
+  zero_d(c->tally_avg, R, c->stream);
+  zero_d(c->tally_var, R, c->stream);
+  c->tally_g = 0;
+  c->vb_nb = 0;
+  CUDA_TRY(cudaGetLastError());
+  return ABX_OK;
+}
+
 // Every batch of every problem of a batch context in one transport launch.
 // Batch b of problem p runs as virtual problem v = p*nb + b: a copy of the
 // problem's settings whose tallies are the b-th copy of the problem's tally
@@ -1838,13 +1907,27 @@ static int ensure_virtual(abx_ctx* c, int nb) {
       u.bin_off += (int64_t)b * (int64_t)R;
       vt[(size_t)b * RT + t] = u;
     }
-  if (c->vprobs) cudaFree(c->vprobs);
-  if (c->vtallies) cudaFree(c->vtallies);
-  c->vprobs = nullptr;
-  c->vtallies = nullptr;
   c->vb_nb = 0;
-  CUDA_TRY(cudaMalloc(&c->vprobs, vp.size() * sizeof(ProbT)));
-  CUDA_TRY(cudaMalloc(&c->vtallies, std::max<size_t>(vt.size(), 1) * sizeof(TallyT)));
+  auto grow = [&](void** ptr, size_t* cap, size_t bytes) -> int {
+    if (*cap >= bytes) return ABX_OK;
+    if (*ptr) cudaFree(*ptr);
+    *ptr = nullptr;
+    *cap = 0;
+    CUDA_TRY(cudaMalloc(ptr, bytes));
+    *cap = bytes;
+    return ABX_OK;
+  };
+  const size_t nv = (size_t)np * nb;
+  int rc;
+  if ((rc = grow((void**)&c->vprobs, &c->vcap[0], vp.size() * sizeof(ProbT))) ||
+      (rc = grow((void**)&c->vtallies, &c->vcap[1], std::max<size_t>(vt.size(), 1) * sizeof(TallyT))) ||
+      (rc = grow((void**)&c->pscore, &c->vcap[2], nv * ABX_PSCORES * sizeof(double))) ||
+      (rc = grow((void**)&c->pcount, &c->vcap[3], nv * ABX_PCOUNTS * sizeof(unsigned long long))) ||
+      (rc = grow((void**)&c->seg_off, &c->vcap[4], (nv + 1) * sizeof(uint64_t))) ||
+      (rc = grow((void**)&c->seg_prob, &c->vcap[5], nv * sizeof(int32_t))) ||
+      (rc = grow((void**)&c->seg_hid0, &c->vcap[6], nv * sizeof(uint64_t))) ||
+      (rc = grow((void**)&c->prun, &c->vcap[7], (size_t)np * sizeof(ProbRun))))
+    return rc;
   CUDA_TRY(cudaMemcpy(c->vprobs, vp.data(), vp.size() * sizeof(ProbT), cudaMemcpyHostToDevice));
   if (!vt.empty()) CUDA_TRY(cudaMemcpy(c->vtallies, vt.data(), vt.size() * sizeof(TallyT), cudaMemcpyHostToDevice));
   const size_t need = std::max<size_t>(R * (size_t)nb, 1);
@@ -1855,20 +1938,6 @@ static int ensure_virtual(abx_ctx* c, int nb) {
     CUDA_TRY(cudaMalloc(&c->tally_gen, need * 8));
     c->tally_gen_cap = need;
   }
-  const size_t nv = (size_t)np * nb;
-  for (void* q : {(void*)c->pscore, (void*)c->pcount, (void*)c->seg_off, (void*)c->seg_prob, (void*)c->seg_hid0})
-    if (q) cudaFree(q);
-  c->pscore = nullptr;
-  c->pcount = nullptr;
-  c->seg_off = nullptr;
-  c->seg_prob = nullptr;
-  c->seg_hid0 = nullptr;
-  CUDA_TRY(cudaMalloc(&c->pscore, nv * ABX_PSCORES * sizeof(double)));
-  CUDA_TRY(cudaMalloc(&c->pcount, nv * ABX_PCOUNTS * sizeof(unsigned long long)));
-  CUDA_TRY(cudaMalloc(&c->seg_off, (nv + 1) * sizeof(uint64_t)));
-  CUDA_TRY(cudaMalloc(&c->seg_prob, nv * sizeof(int32_t)));
-  CUDA_TRY(cudaMalloc(&c->seg_hid0, nv * sizeof(uint64_t)));
-  if (!c->prun) CUDA_TRY(cudaMalloc(&c->prun, (size_t)np * sizeof(ProbRun)));
   // segments: virtual problem v = p*nb + b holds histories b*n_p .. (b+1)*n_p-1
   std::vector<uint64_t> off(nv + 1), hid0(nv);
   std::vector<int32_t> vid(nv);

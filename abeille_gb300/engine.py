@@ -146,6 +146,13 @@ class BatchEngine(Engine):
         self.ctx = C.c_void_p()
         abi.check(self.lib.abx_create_batch(arr, len(self.builts), device, C.byref(self.ctx)), self.lib)
 
+    def replace(self, builts):
+        """Swap in another set of problems, keeping the device buffers."""
+        builts = list(builts)
+        arr = (abi.Problem * len(builts))(*[b.struct for b in builts])
+        self._chk(self.lib.abx_batch_replace(self.ctx, arr, len(builts)))
+        self.builts, self.built, self._arr = builts, builts[0], arr
+
     def run(self, nbatches):
         """Returns (per-problem result dicts, run totals)."""
         res = (abi.ProblemResult * len(self.builts))()

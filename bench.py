@@ -490,7 +490,7 @@ def bench_server(args):
                "p99_ms": float(np.percentile(lat, 99)), "collisions_per_s": coll / (t_end - t0),
                "rounds": st1["rounds"] - st0["rounds"], "busy_ms": st1["busy_ms"] - st0["busy_ms"],
                "transport_ms": st1["transport_ms"] - st0["transport_ms"], "collisions": coll,
-               "round_ms": {k: st1[k + "_ms"] - st0[k + "_ms"] for k in ("create", "run", "readback", "destroy")}}
+               "round_ms": {k: st1[k + "_ms"] - st0[k + "_ms"] for k in ("load", "run", "readback", "free")}}
         if record is not None:
             record.extend(rows)
         return out

@@ -385,6 +385,12 @@ typedef struct abx_problem_result {
  * number the problems' tallies in problem order (`tally_first` above). */
 int abx_create_batch(const abx_problem* problems, int n_problems, int device, abx_ctx** out);
 
+/* Replaces the problems of a batch context (same rules as abx_create_batch;
+ * their tracking and precision must be the context's), keeping its stream and
+ * reusing its device buffers where they are large enough.  On error the
+ * context keeps its previous problems. */
+int abx_batch_replace(abx_ctx* ctx, const abx_problem* problems, int n_problems);
+
 /* Runs `nbatches` batches of every problem of a batch context; `results`
  * (n_problems entries, may be NULL) receives each problem's scores, `stats`
  * (may be NULL) the totals, the transport device time (`transport_ms`) and,
@@ -438,10 +444,10 @@ typedef struct abx_server_stats {
   uint64_t collisions, flights, histories;
   double busy_ms;             /* wall time spent running rounds             */
   double transport_ms;        /* device time inside transport kernels       */
-  double create_ms;           /* of busy_ms: batch context creation         */
+  double load_ms;             /* of busy_ms: loading the round's problems   */
   double run_ms;              /*   running the batches                      */
   double readback_ms;         /*   copying tally bins back                  */
-  double destroy_ms;          /*   freeing the batch context                */
+  double free_ms;             /*   freeing the context after a failed round */
 } abx_server_stats;
 
 int abx_server_create(const abx_server_options* options, abx_server** out);

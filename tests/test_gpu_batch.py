@@ -84,3 +84,22 @@ def test_batch_rejects_mixed_modes():
     with pytest.raises(AbxError) as e:
         BatchEngine([a, m], 0)
     assert e.value.code == 9
+
+
+def test_replace_gives_the_results_of_a_fresh_context():
+    first = [b.build(precision="fp64") for b in (_cap(b) for b in _problems("fp64", 5))]
+    second_b = [_cap(decks.fixed_source_problem(100 + i, precision="fp64", batches=NBATCH)) for i in range(7)]
+    second = [b.build(precision="fp64") for b in second_b]
+    eng = BatchEngine(first, 0)
+    eng.run(NBATCH)
+    eng.replace(second)
+    rows, _ = eng.run(NBATCH)
+    fresh = BatchEngine(second, 0)
+    rows_f, _ = fresh.run(NBATCH)
+    for p, (r, f) in enumerate(zip(rows, rows_f)):
+        assert r["collisions"] == f["collisions"] and r["flights"] == f["flights"], p
+        assert abs(r["leak_avg"] - f["leak_avg"]) <= 1e-12 * abs(f["leak_avg"]), p
+        assert np.allclose(eng.tally(r["tally_first"])["avg"], fresh.tally(f["tally_first"])["avg"],
+                           rtol=1e-12, atol=0), p
+    eng.close()
+    fresh.close()
