@@ -332,7 +332,8 @@ static int append_problem(Pools& P, const abx_problem* pr) {
     P.dg_d.resize(P.dg_d.size() + (size_t)std::max(1, mt.n_delayed));
     discrete_cdf(dgp, mt.n_delayed, P.dg_d.data() + M.dg_off);
     // angle tables
-    M.ang_off = (int)P.ang_hdr.size();
+    const size_t hdr0 = P.ang_hdr.size(), ang0 = P.ang_d.size();
+    M.ang_off = (int)hdr0;
     M.iso = 1;
     for (int gi = 0; gi < G; gi++)
       for (int go = 0; go < G; go++) {
@@ -363,6 +364,12 @@ static int append_problem(Pools& P, const abx_problem* pr) {
         P.ang_d.insert(P.ang_d.end(), cc.begin(), cc.end());
         P.ang_hdr.push_back(h);
       }
+    if (M.iso) {
+      // every (g, g') table is the flat one, which sampling inverts directly
+      P.ang_hdr.resize(hdr0);
+      P.ang_d.resize(ang0);
+      M.ang_off = -1;
+    }
     P.mats.push_back(M);
   }
   // majorant (src/majorant.cpp:132-176)
