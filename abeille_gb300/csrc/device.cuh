@@ -715,7 +715,13 @@ template <class R> ABX_DEV Bound<R> trk_nearest(const Tables& T, const View<R>& 
 // leaves that half-space: infinite when moving inward or parallel, clamped to
 // 0 when the point is already (within rounding) on the far side.  This needs
 // no tolerance and cannot pick a wall the particle is moving away from.
-template <class R> ABX_DEV R exit_dist(const SurfT<R>& s, int32_t t, V3<R> r, V3<R> u) {
+//
+// `on_it`: the particle sits on this surface (the tracker's surface token, set
+// by the crossing or reflection that put it there).  For a quadric the side is
+// then taken from the token and c = 0 exactly: FP32 rounding of c would
+// otherwise put a particle that just crossed outward back inside, and the
+// next flight would cross again at distance 0, back and forth.
+template <class R> ABX_DEV R exit_dist(const SurfT<R>& s, int32_t t, V3<R> r, V3<R> u, bool on_it) {
   const R INF = Tol<R>::INF;
   if (s.type <= ABX_SURF_PLANE) {
     R eval = surf_eval(s, r);
@@ -741,6 +747,13 @@ template <class R> ABX_DEV R exit_dist(const SurfT<R>& s, int32_t t, V3<R> r, V3
   const R a = up * up + uq * uq + uw * uw;
   const R k = p * up + q * uq + w * uw;
   const R c = p * p + q * q + w * w - Rr * Rr;
+  if (on_it) {
+    if (a == R(0)) return INF;  // moving along the surface
+    if (t > 0) return k >= R(0) ? INF : R(0);  // outside: leaves only by turning inward at once
+    if (k > R(0)) return R(0);                 // inside but heading out
+    const R d = R(-2) * k / a;                 // far root with c = 0
+    return d > R(0) ? d : R(0);
+  }
   if (a == R(0)) return ((t < 0) == (c > R(0))) ? R(0) : INF;
   // roots of a s^2 + 2 k s + c = 0; FP64 when the discriminant is small
   // against k^2 (grazing incidence), where FP32 cancellation would dominate
@@ -775,7 +788,7 @@ ABX_DEV void cell_exit(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<R>
     int32_t t = __ldg(rpn + i);
     const SurfT<R> s = V.surf[abs(t) - 1];
     if (bc_only && s.bc == ABX_BC_NORMAL) continue;
-    R d = exit_dist(s, t, r, u);
+    R d = exit_dist(s, t, r, u, t == on);
     if (d < mind) { mind = d; is = -t; }
   }
   dist = mind;

@@ -117,16 +117,27 @@ template <class R> ABX_DEV int group_of(const R* eb, int G, R E) {
   return i;
 }
 
+// Trace records and track-length scoring are called from several places of
+// the loop but run rarely (tracing is a test hook; the track-length tally only
+// exists in some problems).  They are compiled once, out of line, with plain
+// scalar arguments, so the loop's hot code stays compact.
+static __device__ __noinline__ void trace_write(abx_trace_rec* trace, uint64_t cap, unsigned long long* counter,
+                                         uint32_t h, int kind, int g, int cell, uint64_t rng, double rx,
+                                         double ry, double rz, double ux, double uy, double uz, double w) {
+  unsigned long long i = atomicAdd(counter, 1ull);
+  if (i >= cap) return;
+  abx_trace_rec t;
+  t.hist = h; t.kind = kind; t.group = g; t.cell = cell; t.rng_state = rng;
+  t.r[0] = rx; t.r[1] = ry; t.r[2] = rz;
+  t.u[0] = ux; t.u[1] = uy; t.u[2] = uz;
+  t.wgt = w;
+  trace[i] = t;
+}
+
 template <class R> ABX_DEV void trace_rec(const TransportArgs<R>& A, const Lane<R>& L, int kind, int cell) {
   if (L.h >= A.trace_nhist) return;
-  unsigned long long i = atomicAdd(&A.st->trace_n, 1ull);
-  if (i >= A.trace_cap) return;
-  abx_trace_rec t;
-  t.hist = L.h; t.kind = kind; t.group = L.g; t.cell = cell; t.rng_state = L.rng;
-  t.r[0] = (double)L.r.x; t.r[1] = (double)L.r.y; t.r[2] = (double)L.r.z;
-  t.u[0] = (double)L.u.x; t.u[1] = (double)L.u.y; t.u[2] = (double)L.u.z;
-  t.wgt = (double)L.w;
-  A.trace[i] = t;
+  trace_write(A.trace, A.trace_cap, &A.st->trace_n, L.h, kind, L.g, cell, L.rng, (double)L.r.x, (double)L.r.y,
+              (double)L.r.z, (double)L.u.x, (double)L.u.y, (double)L.u.z, (double)L.w);
 }
 
 // Quantity multiplier (src/collision_mesh_tally.cpp:66-100).
@@ -172,15 +183,17 @@ ABX_DEV void score_collision(const Tables& T, const View<R>& V, const ProbT& P, 
 
 // TrackLengthMeshTally::score_flight (src/track_length_mesh_tally.cpp:77-435)
 template <class R>
-ABX_DEV void score_flight(const Tables& T, const View<R>& V, const ProbT& P, const Lane<R>& L, R dfl) {
-  const R* teb = tally_eb<R>(T);
-  for (int ti = P.tally_first; ti < P.tally_first + P.tally_count; ti++) {
-    const TallyT& t = T.tallies[ti];
+__device__ __noinline__ void score_flight_ool(const TallyT* tallies, double* tally_gen, const R* teb, const R* xs,
+                                              const MatT* mats, int tally_first, int tally_count,
+                                              double nparticles, R rx, R ry, R rz, R ux, R uy, R uz, R w, R E,
+                                              int g, int mat, R dfl) {
+  for (int ti = tally_first; ti < tally_first + tally_count; ti++) {
+    const TallyT& t = tallies[ti];
     if (t.est != ABX_EST_TRACK_LENGTH) continue;
     R low[3], hi[3], d[3], dinv[3];
     tally_geom<R>(t, low, hi, d, dinv);
-    V3<R> r = L.r;
-    const V3<R> u = L.u;
+    V3<R> r = mk<R>(rx, ry, rz);
+    const V3<R> u = mk<R>(ux, uy, uz);
     int ijk[3], on[3];
     auto init_idx = [&](V3<R> rr) {
       R rc[3] = {rr.x, rr.y, rr.z}, uc[3] = {u.x, u.y, u.z};
@@ -222,10 +235,16 @@ ABX_DEV void score_flight(const Tables& T, const View<R>& V, const ProbT& P, con
       dd -= dmin;
       init_idx(r);
     }
-    const MatT& M = T.mats[L.mat];
-    R base = R(1) / (R)P.nparticles;
-    base *= qfactor(V, M, t.quantity, L.g, L.w);
-    int l = tally_ebin<R>(teb + t.eb_off, t.ne, L.E);
+    const MatT& M = mats[mat];
+    R base = R(1) / (R)nparticles;
+    switch (t.quantity) {  // src/collision_mesh_tally.cpp:66-100, as qfactor
+      case ABX_Q_ELASTIC: base *= w * xs[M.xs_off + XS_ES * M.G + g]; break;
+      case ABX_Q_ABSORPTION: base *= w * xs[M.xs_off + XS_EABS * M.G + g]; break;
+      case ABX_Q_FISSION: base *= w * xs[M.xs_off + XS_EF * M.G + g]; break;
+      case ABX_Q_TOTAL: base *= w * xs[M.xs_off + XS_ET * M.G + g]; break;
+      default: base *= w;
+    }
+    int l = tally_ebin<R>(teb + t.eb_off, t.ne, E);
     if (l < 0) continue;
     R rem = dd;
     for (int guard = 0; guard < (1 << 22) && rem > R(0); guard++) {
@@ -248,7 +267,7 @@ ABX_DEV void score_flight(const Tables& T, const View<R>& V, const ProbT& P, con
       R dt = dist < rem ? dist : rem;
       if (ijk[0] >= 0 && ijk[0] < t.n[0] && ijk[1] >= 0 && ijk[1] < t.n[1] && ijk[2] >= 0 && ijk[2] < t.n[2]) {
         int64_t idx = t.bin_off + (((int64_t)l * t.n[0] + ijk[0]) * t.n[1] + ijk[1]) * t.n[2] + ijk[2];
-        atomicAdd(T.tally_gen + idx, (double)(dt * base));
+        atomicAdd(tally_gen + idx, (double)(dt * base));
       } else {
         break;
       }
@@ -267,6 +286,12 @@ ABX_DEV void score_flight(const Tables& T, const View<R>& V, const ProbT& P, con
       }
     }
   }
+}
+
+template <class R>
+ABX_DEV void score_flight(const Tables& T, const View<R>& V, const ProbT& P, const Lane<R>& L, R dfl) {
+  score_flight_ool<R>(T.tallies, T.tally_gen, tally_eb<R>(T), V.xs, T.mats, P.tally_first, P.tally_count,
+                      P.nparticles, L.r.x, L.r.y, L.r.z, L.u.x, L.u.y, L.u.z, L.w, L.E, L.g, L.mat, dfl);
 }
 
 // MGAngleDistribution::sample_mu (include/materials/mg_angle_distribution.hpp:45-60,92-101)

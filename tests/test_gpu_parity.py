@@ -190,3 +190,61 @@ def test_errors_leave_the_context_usable():
     assert np.array_equal(sg["parent_daughter_id"], sc["parent_daughter_id"])
     with pytest.raises(AbxError):
         eng.transport(bank, 1.0, True, site_capacity=1)
+
+
+def test_mixed_precision_statistics_config1():
+    """Config 1 (51x51 pins, 10 axial zones, 51x51x20 flux tally) at 2e5
+    histories per generation, 10 inactive + 40 active generations: the mixed
+    mode against FP64 over independent replicas (k within 2 sigma; flux bins
+    with |z| < 2 at the rate two FP64 replica sets reach between themselves,
+    printed beside it)."""
+    R = 12
+    res = {}
+    for prec in ("fp64", "mixed"):
+        ks, avgs = [], []
+        for rep in range(R):
+            b = decks.config1(nparticles=200000)
+            b.seed = 5000 + rep
+            eng = Engine(b.build(precision=prec), 0)
+            st, _, _ = eng.run_power_iteration(50, 10)
+            ks.append(st["kcol_avg"])
+            avgs.append(eng.tally(0)["avg"])
+            eng.close()
+        res[prec] = (np.array(ks), np.array(avgs))
+    (k64, a64), (k32, a32) = res["fp64"], res["mixed"]
+    dk = (k32.mean() - k64.mean()) / np.sqrt(k32.var(ddof=1) / R + k64.var(ddof=1) / R)
+    keep = (a64.mean(0) > 0) & (a32.mean(0) > 0)
+
+    def frac(a, b):
+        z = (a.mean(0) - b.mean(0)) / np.sqrt(a.var(0, ddof=1) / len(a) + b.var(0, ddof=1) / len(b))
+        return np.mean(np.abs(z[keep]) < 2)
+
+    f = frac(a32, a64)
+    control = frac(a64[: R // 2], a64[R // 2:])
+    print(f"config 1 mixed vs fp64: dk = {dk:.2f} sigma, {f:.3f} of {keep.sum()} bins with |z| < 2 "
+          f"(fp64 vs fp64 control: {control:.3f})")
+    assert abs(dk) < 2, (k32.mean(), k64.mean(), dk)
+    assert f >= 0.92
+
+
+@pytest.mark.parametrize("tracking", ["surface-tracking", "delta-tracking"])
+def test_mixed_config2_tracks_like_fp64(tracking):
+    """Config 2 (nested cylinders r = 0.41/0.42/0.475 in every pin, 70 groups,
+    P1) in the mixed mode: no particle may bounce between the surfaces of the
+    thin gap ring; almost none is lost, and flights and collisions per history
+    stay within 2 % of the FP64 path's (statistical quantities, different
+    rounding)."""
+    out = {}
+    for prec in ("fp64", "mixed"):
+        b = decks.config2(nparticles=20000, tracking=tracking)
+        eng = Engine(b.build(precision=prec), 0)
+        st, recs = eng.run_power_iteration_records(4, 0)
+        out[prec] = (sum(r["flights"] for r in recs), sum(r["collisions"] for r in recs),
+                     sum(r["histories"] for r in recs), sum(r["lost"] for r in recs))
+        eng.close()
+    f64, c64, h64, l64 = out["fp64"]
+    f32, c32, h32, l32 = out["mixed"]
+    assert l64 == 0
+    assert l32 <= 1e-4 * h32, out
+    assert abs(f32 / h32 - f64 / h64) <= 0.02 * f64 / h64, out
+    assert abs(c32 / h32 - c64 / h64) <= 0.02 * c64 / h64, out
