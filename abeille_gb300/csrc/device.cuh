@@ -869,7 +869,11 @@ template <class R> ABX_DEV Bound<R> trk_nearest_mixed(const Tables& T, const Vie
         int t[3];
         tile_unpack(k.gettile(i), t);
         R d = tile_exit(V.lat[T.univ[id].lat], rl, k.u, t);
-        if (d < b.dist) { b.dist = d; b.btype = ABX_BC_NORMAL; b.si = -1; b.token = 0; }
+        // A tile wall that coincides with a boundary-condition surface (a
+        // lattice filling its outer box) is that surface; FP32 rounding of the
+        // two distances must not hand the tie to the tile wall.
+        const bool bc_tie = b.si >= 0 && b.btype != ABX_BC_NORMAL && d > b.dist - Tol<R>::TILE;
+        if (d < b.dist && !bc_tie) { b.dist = d; b.btype = ABX_BC_NORMAL; b.si = -1; b.token = 0; }
       } else if (ty == PAD_CELL) {
         R d; int32_t ts;
         cell_exit(T, V, id, rl, k.u, k.token, false, d, ts);

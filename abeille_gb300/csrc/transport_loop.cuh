@@ -153,6 +153,7 @@ __global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R
   {                                                                                             \
     nlost++;                                                                                    \
     if (A.pcount) atomicAdd(A.pcount + (size_t)L.pid * ABX_PCOUNTS + 3, 1ull);                  \
+    if (TRACE) trace_rec(A, L, 7, k.cell);                                                      \
   }
 
   while (true) {

@@ -473,7 +473,8 @@ int abx_server_get_stats(abx_server* server, abx_server_stats* stats);
  * records); *n_out receives the count.  Pass n_hist = 0 to disable. */
 typedef struct abx_trace_rec {
   uint32_t hist;
-  int32_t kind;  /* 0 flight-virtual 1 flight-real 2 leak 3 reflect 4 collision-done 5 cross */
+  int32_t kind;  /* 0 flight-virtual 1 flight-real 2 leak 3 reflect 4 collision-done 5 cross
+                    6 resurrect 7 lost (mixed mode: counted and ended)              */
   int32_t group;
   int32_t cell;
   uint64_t rng_state;
