@@ -107,8 +107,10 @@ ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& ac
   }
 }
 
+// Occupancy: three 256-thread blocks per SM in FP32 tracking (80 registers),
+// two in FP64 (128 registers).
 template <class R, int TRACK>
-__global__ void __launch_bounds__(256, 2) transport_kernel(const TransportArgs<R> A) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) transport_kernel(const TransportArgs<R> A) {
   const bool TRACE = A.trace != nullptr;
   const Tables& T = A.T;
   const View<R> V = make_view<R>(T);
