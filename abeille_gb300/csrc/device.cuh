@@ -890,16 +890,23 @@ template <class R> ABX_DEV Bound<R> trk_nearest_mixed(const Tables& T, const Vie
 }
 
 // rotate_direction (include/utils/direction.hpp:130-151)
+// In FP32 a cosine can round just outside [-1, 1]; the square roots then take
+// a clamped argument (FP64 keeps the reference's expressions unchanged).
+template <class R> ABX_DEV R sqrt_1m(R x2) {
+  const R a = R(1) - x2;
+  return m_sqrt(sizeof(R) == 4 && a < R(0) ? R(0) : a);
+}
+
 template <class R> ABX_DEV V3<R> rotate(V3<R> u, R mu, R c, R s) {
-  R sqrt_mu = m_sqrt(R(1) - mu * mu);
-  R sqrt_w = m_sqrt(R(1) - u.z * u.z);
+  R sqrt_mu = sqrt_1m<R>(mu * mu);
+  R sqrt_w = sqrt_1m<R>(u.z * u.z);
   R ux, uy, uz;
   if (sqrt_w > Tol<R>::ROT) {
     ux = mu * u.x + sqrt_mu * (u.x * u.z * c - u.y * s) / sqrt_w;
     uy = mu * u.y + sqrt_mu * (u.y * u.z * c + u.x * s) / sqrt_w;
     uz = mu * u.z - sqrt_mu * sqrt_w * c;
   } else {
-    R sqrt_v = m_sqrt(R(1) - u.y * u.y);
+    R sqrt_v = sqrt_1m<R>(u.y * u.y);
     ux = mu * u.x + sqrt_mu * (u.x * u.y * c + u.z * s) / sqrt_v;
     uy = mu * u.y - sqrt_mu * sqrt_v * c;
     uz = mu * u.z + sqrt_mu * (u.y * u.z * c - u.x * s) / sqrt_v;

@@ -310,9 +310,17 @@ ABX_DEV R sample_mu(const Tables& T, const View<R>& V, const MatT& M, int gi, in
   int l = lower_bound<R>(cdf, a.n, xi);
   if (xi == cdf[l]) return mu[l];
   l--;
-  if (pdf[l] == pdf[l + 1]) return mu[l] + ((xi - cdf[l]) / pdf[l]);
-  R m = (pdf[l + 1] - pdf[l]) / (mu[l + 1] - mu[l]);
-  return mu[l] + (R(1) / m) * (m_sqrt(pdf[l] * pdf[l] + R(2) * m * (xi - cdf[l])) - pdf[l]);
+  R out;
+  if (pdf[l] == pdf[l + 1]) {
+    out = mu[l] + ((xi - cdf[l]) / pdf[l]);
+  } else {
+    R m = (pdf[l + 1] - pdf[l]) / (mu[l + 1] - mu[l]);
+    R arg = pdf[l] * pdf[l] + R(2) * m * (xi - cdf[l]);
+    if (sizeof(R) == 4 && arg < R(0)) arg = R(0);
+    out = mu[l] + (R(1) / m) * (m_sqrt(arg) - pdf[l]);
+  }
+  if (sizeof(R) == 4) out = out < R(-1) ? R(-1) : (out > R(1) ? R(1) : out);  // FP32 rounding
+  return out;
 }
 
 template <class R> ABX_DEV R group_mid(const View<R>& V, const ProbT& P, int g) {

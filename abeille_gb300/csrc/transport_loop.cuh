@@ -371,6 +371,11 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) transport_kernel(
       ncoll++;
       L.hcoll++;
       collide(A, T, V, P, L, acc, converged, kcol, alive);
+      if (sizeof(R) == 4 && !(m_abs(L.u.x) <= R(1) && m_abs(L.u.y) <= R(1) && m_abs(L.u.z) <= R(1))) {
+        // mixed mode: a direction that is not finite cannot be tracked
+        ABX_LOST();
+        alive = false;
+      }
       k.u = L.u;
       if (TRACE) trace_rec(A, L, 4, k.cell);
       ph = alive ? PH_FLIGHT : PH_DEAD;
