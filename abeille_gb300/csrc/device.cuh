@@ -848,7 +848,23 @@ template <class R> ABX_DEV Bound<R> trk_bc_mixed(const Tables& T, const View<R>&
             ui = U.outer;
             continue;
           }
-          for (int j = 0; j < U.list_len; j++) b = cells_bc_mixed(T, V, __ldg(T.cell_lists + U.list_off + j), rl, k.u, k.token, b);
+          if (U.bc_len >= 0) {
+            // each distinct boundary half-space once, not once per cell
+            for (int j = 0; j < U.bc_len; j++) {
+              const int32_t t = __ldg(T.rpn + U.bc_off + j);
+              const SurfT<R> s = V.surf[abs(t) - 1];
+              const R d = exit_dist(s, t, rl, k.u, t == k.token);
+              if (d < b.dist) {
+                b.dist = d;
+                b.si = abs(t) - 1;
+                b.token = t;
+                b.btype = s.bc;
+              }
+            }
+          } else {
+            for (int j = 0; j < U.list_len; j++)
+              b = cells_bc_mixed(T, V, __ldg(T.cell_lists + U.list_off + j), rl, k.u, k.token, b);
+          }
           break;
         }
       }

@@ -273,6 +273,30 @@ static int append_problem(Pools& P, const abx_problem* pr) {
     }
     P.univ.push_back(t);
   }
+  // distinct boundary-condition tokens per cell universe (mixed-mode search)
+  for (int i = univ0; i < (int)P.univ.size(); i++) {
+    UnivT& U = P.univ[i];
+    U.bc_off = (int)P.rpn.size();
+    U.bc_len = 0;
+    if (U.kind != ABX_UNIV_CELLS || !U.has_bc) continue;
+    std::vector<int32_t> toks;
+    for (int j = 0; j < U.list_len && U.bc_len >= 0; j++) {
+      const CellT& c = P.cells[P.cell_lists[U.list_off + j]];
+      if (!c.has_bc) continue;
+      if (!c.simple) {
+        U.bc_len = -1;
+        break;
+      }
+      for (int k = 0; k < c.rpn_len; k++) {
+        const int32_t t = P.rpn[c.rpn_off + k];
+        if (P.surf_d[std::abs(t) - 1].bc == ABX_BC_NORMAL) continue;
+        if (std::find(toks.begin(), toks.end(), t) == toks.end()) toks.push_back(t);
+      }
+    }
+    if (U.bc_len < 0) continue;
+    P.rpn.insert(P.rpn.end(), toks.begin(), toks.end());
+    U.bc_len = (int)toks.size();
+  }
   // lattices inherit their outer universe's boundary flag (src/lattice.cpp:45-53)
   for (int pass = 0; pass < 16; pass++)
     for (int i = univ0; i < (int)P.univ.size(); i++)

@@ -36,7 +36,10 @@ struct UnivT {
   int32_t outer;
   int32_t has_bc;
   int32_t lat;  // index into the lattice parameter pool
-  int32_t pad_;
+  // distinct boundary-condition half-spaces of the universe's cells (region
+  // tokens in the rpn pool), or bc_len = -1 when a cell is not a plain
+  // intersection; used by the mixed-mode boundary search
+  int32_t bc_off, bc_len;
 };
 
 // Per material: xs block (7 rows of G: Et, Eabs, Ef, nu_tot, nu_d, Es, vEf),

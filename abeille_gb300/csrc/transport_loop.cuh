@@ -107,10 +107,12 @@ ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& ac
   }
 }
 
-// Occupancy: three 256-thread blocks per SM in FP32 tracking (80 registers),
-// two in FP64 (128 registers).
+// Occupancy (measured on config 1 and config 2): FP32 delta tracking runs four
+// 256-thread blocks per SM (64 registers), FP32 surface tracking three (80
+// registers), FP64 two (128 registers).
 template <class R, int TRACK>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) transport_kernel(const TransportArgs<R> A) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK == ABX_TRACK_DELTA ? 4 : 3) : 2)
+    transport_kernel(const TransportArgs<R> A) {
   const bool TRACE = A.trace != nullptr;
   const Tables& T = A.T;
   const View<R> V = make_view<R>(T);
