@@ -361,7 +361,8 @@ ABX_DEV void collide(const TransportArgs<R>& A, const Tables& T, const View<R>& 
     R P_delayed = xs[XS_NUD * G + g] / nu;
     uint64_t base = 0;
     const bool keig = P.mode == ABX_MODE_K_EIGENVALUE;
-    if (keig) {
+    if (keig && __any_sync(__activemask(), n_new > 0)) {
+      // one atomic per warp reserves the sites of every colliding lane
       cg::coalesced_group grp = cg::coalesced_threads();
       unsigned my = (unsigned)n_new;
       unsigned pre = cg::exclusive_scan(grp, my);
