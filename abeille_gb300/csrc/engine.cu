@@ -856,6 +856,7 @@ __global__ void k_next_bank(SiteT<R> S, DevState* st, const uint32_t* off, BankT
   const double W = (double)st->site_pos - (double)st->site_neg;
   const double wpp = P.nparticles / W;
   const unsigned long long g0 = run->global_hist;
+  double w_in_mesh = 0.;  // this thread's share of the entropy total
   for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < ns && j < cap;
        j += (unsigned long long)gridDim.x * blockDim.x) {
     uint32_t h = S.hist[j];
@@ -877,10 +878,16 @@ __global__ void k_next_bank(SiteT<R> S, DevState* st, const uint32_t* off, BankT
       int ny = (int)floor(((double)y - P.ent_low[1]) / P.ent_d[1]);
       int nz = (int)floor(((double)z - P.ent_low[2]) / P.ent_d[2]);
       if (nx >= 0 && nx < P.ent_shape[0] && ny >= 0 && ny < P.ent_shape[1] && nz >= 0 && nz < P.ent_shape[2]) {
-        atomicAdd(ent_total, (double)ws);
+        w_in_mesh += (double)ws;
         atomicAdd(ent_bins + ((size_t)P.ent_shape[1] * P.ent_shape[2] * nx + (size_t)P.ent_shape[2] * ny + nz), (double)ws);
       }
     }
+  }
+  // the entropy total: one atomic per warp instead of one per site on a
+  // single address
+  if (P.ent_on) {
+    for (int o = 16; o > 0; o >>= 1) w_in_mesh += __shfl_down_sync(0xffffffffu, w_in_mesh, o);
+    if ((threadIdx.x & 31u) == 0 && w_in_mesh != 0.) atomicAdd(ent_total, w_in_mesh);
   }
 }
 

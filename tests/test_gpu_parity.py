@@ -143,37 +143,53 @@ def test_reference_known_answers_on_gpu(name, precision):
     assert abs(st["kcol_avg"] - deck["_expected_k"]) < 4 * st["kcol_std"] + 2e-4, st
 
 
+def _replicas(builder_fn, prec, seed0, R, ngen, nign):
+    ks, avgs = [], []
+    for rep in range(R):
+        b = builder_fn()
+        b.seed = seed0 + rep
+        eng = Engine(b.build(precision=prec), 0)
+        st, _, _ = eng.run_power_iteration(ngen, nign)
+        ks.append(st["kcol_avg"])
+        avgs.append(eng.tally(0)["avg"])
+        eng.close()
+    return np.array(ks), np.array(avgs)
+
+
+def _agreement(x, y, keep=None):
+    """k difference in sigma, fraction of bins with |z| < 2 and mean z between
+    two replica sets (sigma of each mean from its replica spread)."""
+    (kx, ax), (ky, ay) = x, y
+    dk = (kx.mean() - ky.mean()) / np.sqrt(kx.var(ddof=1) / len(kx) + ky.var(ddof=1) / len(ky))
+    z = (ax.mean(0) - ay.mean(0)) / np.sqrt(ax.var(0, ddof=1) / len(ax) + ay.var(0, ddof=1) / len(ay))
+    if keep is not None:
+        z = z[keep]
+    return dk, np.mean(np.abs(z) < 2), z.mean()
+
+
 def test_mixed_precision_statistics_config0():
-    """FP32 tracking / FP64 tallies against the FP64 path: k within 2 sigma and
-    flux bins with |z| < 2.
+    """FP32 tracking / FP64 tallies against the FP64 path on config 0: k within
+    2 sigma, and flux bins with |z| < 2 at the rate two independent FP64
+    replica sets reach between themselves.
 
     The standard deviations come from independent replicas (different seeds):
     generation-to-generation statistics of one power iteration underestimate
-    the error because successive generations are correlated (two FP64 runs
-    with different seeds already put only ~89 % of config-0 bins inside
-    |z| < 2 with those).  With 24 replicas per precision the expected fraction
-    under agreement is ~0.95 with a binomial spread of ~0.013 over 289 bins,
-    so the bar is 0.92."""
+    the error because successive generations are correlated.  The 289 bins
+    share one fission source, so the fraction of bins with |z| < 2 moves by
+    several percent from one replica set to another (FP64 against FP64 gives
+    0.89 to 0.97); the bar is therefore set against an FP64/FP64 control
+    computed in the same test, and the mean z must stay near 0."""
     R = 24
-    res = {}
-    for prec in ("fp64", "mixed"):
-        ks, avgs = [], []
-        for rep in range(R):
-            b = decks.config0(nparticles=5000)
-            b.seed = 1000 + rep
-            eng = Engine(b.build(precision=prec), 0)
-            st, _, _ = eng.run_power_iteration(40, 10)
-            ks.append(st["kcol_avg"])
-            avgs.append(eng.tally(0)["avg"])
-            eng.close()
-        res[prec] = (np.array(ks), np.array(avgs))
-    (k64, a64), (k32, a32) = res["fp64"], res["mixed"]
-    dk = (k32.mean() - k64.mean()) / np.sqrt(k32.var(ddof=1) / R + k64.var(ddof=1) / R)
-    assert abs(dk) < 2, (k32.mean(), k64.mean(), dk)
-    z = (a32.mean(0) - a64.mean(0)) / np.sqrt(a32.var(0, ddof=1) / R + a64.var(0, ddof=1) / R)
-    frac = np.mean(np.abs(z) < 2)
-    print(f"mixed vs fp64: dk = {dk:.2f} sigma, {frac:.3f} of {z.size} bins with |z| < 2")
-    assert frac >= 0.92
+    fp64_a = _replicas(lambda: decks.config0(nparticles=5000), "fp64", 1000, R, 40, 10)
+    fp64_b = _replicas(lambda: decks.config0(nparticles=5000), "fp64", 5000, R, 40, 10)
+    mixed = _replicas(lambda: decks.config0(nparticles=5000), "mixed", 9000, R, 40, 10)
+    dk, frac, mz = _agreement(mixed, fp64_a)
+    dk_c, frac_c, mz_c = _agreement(fp64_b, fp64_a)
+    print(f"mixed vs fp64: dk = {dk:.2f} sigma, {frac:.3f} of bins |z| < 2, mean z {mz:+.3f}; "
+          f"fp64 vs fp64 control: dk = {dk_c:.2f}, {frac_c:.3f}, mean z {mz_c:+.3f}")
+    assert abs(dk) < 2, dk
+    assert frac >= 0.85 and frac >= frac_c - 0.08, (frac, frac_c)
+    assert abs(mz) < 0.3, mz
 
 
 def test_errors_leave_the_context_usable():
@@ -195,36 +211,21 @@ def test_errors_leave_the_context_usable():
 def test_mixed_precision_statistics_config1():
     """Config 1 (51x51 pins, 10 axial zones, 51x51x20 flux tally) at 2e5
     histories per generation, 10 inactive + 40 active generations: the mixed
-    mode against FP64 over independent replicas (k within 2 sigma; flux bins
-    with |z| < 2 at the rate two FP64 replica sets reach between themselves,
-    printed beside it)."""
+    mode against FP64 over independent replicas, with an FP64/FP64 control
+    (same criteria as config 0)."""
     R = 12
-    res = {}
-    for prec in ("fp64", "mixed"):
-        ks, avgs = [], []
-        for rep in range(R):
-            b = decks.config1(nparticles=200000)
-            b.seed = 5000 + rep
-            eng = Engine(b.build(precision=prec), 0)
-            st, _, _ = eng.run_power_iteration(50, 10)
-            ks.append(st["kcol_avg"])
-            avgs.append(eng.tally(0)["avg"])
-            eng.close()
-        res[prec] = (np.array(ks), np.array(avgs))
-    (k64, a64), (k32, a32) = res["fp64"], res["mixed"]
-    dk = (k32.mean() - k64.mean()) / np.sqrt(k32.var(ddof=1) / R + k64.var(ddof=1) / R)
-    keep = (a64.mean(0) > 0) & (a32.mean(0) > 0)
-
-    def frac(a, b):
-        z = (a.mean(0) - b.mean(0)) / np.sqrt(a.var(0, ddof=1) / len(a) + b.var(0, ddof=1) / len(b))
-        return np.mean(np.abs(z[keep]) < 2)
-
-    f = frac(a32, a64)
-    control = frac(a64[: R // 2], a64[R // 2:])
-    print(f"config 1 mixed vs fp64: dk = {dk:.2f} sigma, {f:.3f} of {keep.sum()} bins with |z| < 2 "
-          f"(fp64 vs fp64 control: {control:.3f})")
-    assert abs(dk) < 2, (k32.mean(), k64.mean(), dk)
-    assert f >= 0.92
+    mk = lambda: decks.config1(nparticles=200000)  # noqa: E731
+    fp64_a = _replicas(mk, "fp64", 5000, R, 50, 10)
+    fp64_b = _replicas(mk, "fp64", 7000, R // 2, 50, 10)
+    mixed = _replicas(mk, "mixed", 9000, R, 50, 10)
+    keep = (fp64_a[1].mean(0) > 0) & (mixed[1].mean(0) > 0)
+    dk, frac, mz = _agreement(mixed, fp64_a, keep)
+    dk_c, frac_c, mz_c = _agreement(fp64_b, fp64_a, keep)
+    print(f"config 1 mixed vs fp64: dk = {dk:.2f} sigma, {frac:.3f} of {keep.sum()} bins |z| < 2, mean z {mz:+.3f}; "
+          f"fp64 vs fp64 control: dk = {dk_c:.2f}, {frac_c:.3f}, mean z {mz_c:+.3f}")
+    assert abs(dk) < 2, dk
+    assert frac >= 0.85 and frac >= frac_c - 0.08, (frac, frac_c)
+    assert abs(mz) < 0.3, mz
 
 
 @pytest.mark.parametrize("tracking", ["surface-tracking", "delta-tracking"])
