@@ -6,8 +6,8 @@
 
 namespace abx {
 
-template __global__ void transport_kernel<double, ABX_TRACK_DELTA>(const TransportArgs<double>);
-template __global__ void transport_kernel<double, ABX_TRACK_SURFACE>(const TransportArgs<double>);
+template __global__ void transport_kernel<double, ABX_TRACK_DELTA>(const __grid_constant__ TransportArgs<double>);
+template __global__ void transport_kernel<double, ABX_TRACK_SURFACE>(const __grid_constant__ TransportArgs<double>);
 
 void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace, int grid, int block,
                         cudaStream_t s) {

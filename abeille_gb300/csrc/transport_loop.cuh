@@ -90,6 +90,13 @@ ABX_DEV void reflect_move(const View<R>& V, Trk<R>& k, Lane<R>& L, const Bound<R
   if (sizeof(R) == 4) k.token = side;
 }
 
+// rare and long: the boundary-condition search runs out of line
+template <class R>
+__device__ __noinline__ Bound<R> trk_bc_ool(const Tables& T, const ProbT& P, const Trk<R>& k) {
+  const View<R> V = make_view<R>(T);
+  return sizeof(R) == 8 ? trk_bc(T, V, P, k) : trk_bc_mixed(T, V, P, k);
+}
+
 // End of a history: its fission-site count (for the bank sort) and its score
 // totals, to the block's accumulators or, in a batch of problems, to its
 // problem's sums and counters.
@@ -112,7 +119,7 @@ ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& ac
 // registers), FP64 two (128 registers).
 template <class R, int TRACK>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK == ABX_TRACK_DELTA ? 4 : 3) : 2)
-    transport_kernel(const TransportArgs<R> A) {
+    transport_kernel(const __grid_constant__ TransportArgs<R> A) {
   const bool TRACE = A.trace != nullptr;
   const Tables& T = A.T;
   const View<R> V = make_view<R>(T);
@@ -345,7 +352,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK == ABX_TRACK_DELT
     // -------------------------------------------------------------- boundary
     if (ph == PH_LOST) {
       const ProbT& P = T.probs[L.pid];
-      const Bound<R> b = sizeof(R) == 8 ? trk_bc(T, V, P, k) : trk_bc_mixed(T, V, P, k);
+      const Bound<R> b = trk_bc_ool<R>(T, P, k);
       if (converged && P.has_tle) score_flight(T, V, P, L, dcol < b.dist ? dcol : b.dist);
       if (b.btype == ABX_BC_VACUUM) {
         acc.hleak += L.w;

@@ -5,8 +5,8 @@
 
 namespace abx {
 
-template __global__ void transport_kernel<float, ABX_TRACK_DELTA>(const TransportArgs<float>);
-template __global__ void transport_kernel<float, ABX_TRACK_SURFACE>(const TransportArgs<float>);
+template __global__ void transport_kernel<float, ABX_TRACK_DELTA>(const __grid_constant__ TransportArgs<float>);
+template __global__ void transport_kernel<float, ABX_TRACK_SURFACE>(const __grid_constant__ TransportArgs<float>);
 
 void launch_transport_f(const TransportArgs<float>& A, int tracking, bool trace, int grid, int block,
                         cudaStream_t s) {
