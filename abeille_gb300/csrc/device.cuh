@@ -276,17 +276,23 @@ template <class R> ABX_DEV R surf_dist(const SurfT<R>& s, V3<R> r, V3<R> u, bool
 }
 
 // ----------------------------------------------------------------- cells
-// Cell::is_inside_simple / is_inside_complex (src/cell.cpp:147-199)
+// Cell::is_inside_simple / is_inside_complex (src/cell.cpp:147-199).
+// Called from the validity check after every flight and from the descent;
+// compiled once, out of line, with pointer arguments: one copy of the
+// surface-sign code instead of one per caller measurably cuts the loop's
+// instruction-fetch stalls.
 template <class R>
-ABX_DEV bool cell_inside(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<R> u, int32_t on) {
-  const CellT c = T.cells[ci];
-  const int32_t* __restrict__ rpn = T.rpn + c.rpn_off;
+__device__ __noinline__ bool cell_inside_at(const CellT* __restrict__ cells, const int32_t* __restrict__ rpn_pool,
+                                            const SurfT<R>* __restrict__ surf, int ci, V3<R> r, V3<R> u,
+                                            int32_t on) {
+  const CellT c = cells[ci];
+  const int32_t* __restrict__ rpn = rpn_pool + c.rpn_off;
   if (c.simple) {
     for (int i = 0; i < c.rpn_len; i++) {
       int32_t t = __ldg(rpn + i);
       if (t == on) continue;
       if (-t == on) return false;
-      int sg = surf_sign(V.surf[abs(t) - 1], r, u);
+      int sg = surf_sign(surf[abs(t) - 1], r, u);
       if ((sg > 0 && t < 0) || (sg < 0 && t > 0)) return false;
     }
     return true;
@@ -308,7 +314,7 @@ ABX_DEV bool cell_inside(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<
       if (t == on) v = true;
       else if (-t == on) v = false;
       else {
-        int sg = surf_sign(V.surf[abs(t) - 1], r, u);
+        int sg = surf_sign(surf[abs(t) - 1], r, u);
         v = (sg > 0 && t > 0) || (sg < 0 && t < 0);
       }
       st = (st & ~(1ull << sp)) | ((uint64_t)v << sp);
@@ -316,6 +322,11 @@ ABX_DEV bool cell_inside(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<
   }
   if (sp == 0) return (st & 1u) != 0;
   return true;
+}
+
+template <class R>
+ABX_DEV bool cell_inside(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<R> u, int32_t on) {
+  return cell_inside_at<R>(T.cells, T.rpn, V.surf, ci, r, u, on);
 }
 
 // Cell::distance_to_boundary / distance_to_boundary_condition (src/cell.cpp:79-141)
