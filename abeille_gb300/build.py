@@ -1,12 +1,13 @@
 """In-tree build of the CUDA engine (sm_103a) into abeille_gb300/_lib/.
 
-Four translation units are compiled in parallel with nvcc and linked into one
+Five translation units are compiled in parallel with nvcc and linked into one
 shared library exposing the C-ABI of include/abeille_gb300.h:
 
-  engine.cu           host side + bookkeeping kernels     --fmad=false
-  transport_fp64.cu   FP64 parity transport kernels        --fmad=false
-  transport_mixed.cu  FP32-tracking transport kernels
-  server.cpp          request loop (host scheduler thread)
+  engine.cu                   host side + bookkeeping kernels     --fmad=false
+  transport_fp64.cu           FP64 parity transport kernels        --fmad=false
+  transport_mixed.cu          FP32-tracking kernels, delta tracking
+  transport_mixed_surface.cu  FP32-tracking kernels, surface tracking
+  server.cpp                  request loop (host scheduler thread)
 
 Host code is compiled with -ffp-contract=off so derived tables round the same
 way on x86-64 and AArch64.  A stamp of the sources and flags skips rebuilds.
@@ -30,6 +31,7 @@ UNITS = [
     ("engine.cu", ["--fmad=false"]),
     ("transport_fp64.cu", ["--fmad=false"]),
     ("transport_mixed.cu", []),
+    ("transport_mixed_surface.cu", []),
     ("server.cpp", []),
 ]
 

@@ -700,6 +700,7 @@ struct abx_context {
   double last_ms = 0.;
   uint64_t max_events = 10000000ull;
   int prec = ABX_PREC_FP64;
+  bool all_iso = false;  // every material scatters isotropically
   void* flush = nullptr;
   size_t flush_bytes = 0;
   // batches of problems
@@ -1168,7 +1169,7 @@ template <class R> static TransportArgs<R> make_args(abx_ctx* c, const BankT<R>&
 static int launch_transport(abx_ctx* c, bool mixed, int which_bank, size_t site_cap) {
   if (mixed) {
     TransportArgs<float> A = make_args<float>(c, c->bf[which_bank].b, c->sf.s, site_cap);
-    launch_transport_f(A, c->prob0.tracking, c->trace_nhist > 0, c->grid, c->block, c->stream);
+    launch_transport_f(A, c->prob0.tracking, c->all_iso, c->trace_nhist > 0, c->grid, c->block, c->stream);
   } else {
     TransportArgs<double> A = make_args<double>(c, c->bd[which_bank].b, c->sd.s, site_cap);
     launch_transport_d(A, c->prob0.tracking, c->trace_nhist > 0, c->grid, c->block, c->stream);
@@ -1220,6 +1221,8 @@ static int create_ctx(const abx_problem* problems, int nprob, int device, abx_ct
   }
   c->prob0 = c->P.probs[0];
   for (const MatT& m : c->P.mats) c->fissile_any |= m.fissile != 0;
+  c->all_iso = true;
+  for (const MatT& m : c->P.mats) c->all_iso = c->all_iso && m.iso != 0;
   const int prec = problem->settings.precision;
   if (prec != ABX_PREC_FP64 && prec != ABX_PREC_MIXED) {
     delete c;
@@ -1262,7 +1265,7 @@ static int create_ctx(const abx_problem* problems, int nprob, int device, abx_ct
   int block = problem->settings.block_size > 0 ? problem->settings.block_size : 256;
   block = std::max(32, std::min(256, block / 32 * 32));
   c->block = block;
-  int occ = prec == ABX_PREC_MIXED ? occupancy_f(c->prob0.tracking, block) : occupancy_d(c->prob0.tracking, block);
+  int occ = prec == ABX_PREC_MIXED ? occupancy_f(c->prob0.tracking, c->all_iso, block) : occupancy_d(c->prob0.tracking, block);
   if (occ < 1) occ = 1;
   c->grid = c->nsm * occ;
   if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(ABX_ERR_CUDA, "device sync failed"));
@@ -1461,7 +1464,7 @@ static int transport_noalloc_impl(abx_ctx* c, unsigned char* scratch, const abx_
   A.st = c->st;
   A.trace = nullptr;
   A.max_events = c->max_events;
-  if constexpr (sizeof(R) == 4) launch_transport_f(A, c->prob0.tracking, false, c->grid, c->block, c->stream);
+  if constexpr (sizeof(R) == 4) launch_transport_f(A, c->prob0.tracking, c->all_iso, false, c->grid, c->block, c->stream);
   else launch_transport_d(A, c->prob0.tracking, false, c->grid, c->block, c->stream);
   CUDA_TRY(cudaGetLastError());
   unsigned nb = (unsigned)((n + SCAN_CHUNK - 1) / SCAN_CHUNK);
@@ -1892,6 +1895,8 @@ extern "C" int abx_batch_replace(abx_ctx* c, const abx_problem* problems, int n_
   c->prob0 = c->P.probs[0];
   c->fissile_any = false;
   for (const MatT& m : c->P.mats) c->fissile_any |= m.fissile != 0;
+  c->all_iso = true;
+  for (const MatT& m : c->P.mats) c->all_iso = c->all_iso && m.iso != 0;
   int rc = upload(c->P, c->D);
   if (rc) return rc;
   const size_t R = (size_t)std::max<int64_t>(c->P.tally_bins, 1);

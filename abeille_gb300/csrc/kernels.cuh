@@ -295,10 +295,12 @@ ABX_DEV void score_flight(const Tables& T, const View<R>& V, const ProbT& P, con
 }
 
 // MGAngleDistribution::sample_mu (include/materials/mg_angle_distribution.hpp:45-60,92-101)
-template <class R>
+// ISO: every material of the problem scatters isotropically (the launch
+// picks this instantiation), so the table path is compiled out.
+template <class R, bool ISO>
 ABX_DEV R sample_mu(const Tables& T, const View<R>& V, const MatT& M, int gi, int go, uint64_t& rng) {
   const R xi = canon<R>(rng);
-  if (M.iso) {
+  if (ISO || M.iso) {
     // the two-point {-1,1} table with pdf {0.5,0.5}: histogram branch
     if (xi == R(0)) return R(-1);
     return R(-1) + ((xi - R(0)) / R(0.5));
@@ -327,10 +329,63 @@ template <class R> ABX_DEV R group_mid(const View<R>& V, const ProbT& P, int g) 
   return R(0.5) * (V.ebnd[P.eb_off + g] + V.ebnd[P.eb_off + g + 1]);
 }
 
+// The neutrons of one fission event (Transporter::make_fission_neutrons,
+// src/transporter.cpp:400-487; MGNuclide::sample_fission,
+// src/mg_nuclide.cpp:504-544): per neutron a chi-row draw, an isotropic
+// direction, the delayed test, then the site (k-eigenvalue) or a secondary
+// on the history's stack (fixed source).  A few percent of collisions bank
+// neutrons, so this runs out of line with scalar arguments and hands back
+// the advanced random state.
+struct FissionOut {
+  uint64_t rng;
+  uint32_t nsec;
+};
+
+template <class R>
+__device__ __noinline__ FissionOut fission_neutrons(const TransportArgs<R>& A, const R* chi, const R* ebnd,
+                                                    const R* dgcdf, int G, int ndg, R P_delayed, int n_new,
+                                                    uint64_t base, uint64_t rng, R rx, R ry, R rz, R ux, R uy,
+                                                    R uz, bool positive, uint32_t h, uint32_t dau, uint32_t nsec,
+                                                    bool keig) {
+  const V3<R> u0 = mk<R>(ux, uy, uz);
+  const R wgt = positive ? R(1) : R(-1);
+  for (int i = 0; i < n_new; i++) {
+    int ei = discrete<R>(rng, chi, G);
+    R E_out = R(0.5) * (ebnd[ei] + ebnd[ei + 1]);  // group_mid
+    R mu = R(2) * canon<R>(rng) - R(1);
+    R c, s;
+    azimuth(canon<R>(rng), c, s);
+    V3<R> uo = rotate(u0, mu, c, s);
+    if (canon<R>(rng) < P_delayed) (void)discrete<R>(rng, dgcdf, ndg);
+    if (keig) {
+      uint64_t j = base + i;
+      if (j < A.site_cap) {
+        A.sites.x[j] = rx; A.sites.y[j] = ry; A.sites.z[j] = rz;
+        A.sites.ux[j] = uo.x; A.sites.uy[j] = uo.y; A.sites.uz[j] = uo.z;
+        A.sites.E[j] = E_out; A.sites.w[j] = wgt;
+        A.sites.hist[j] = h; A.sites.dau[j] = dau + (uint32_t)i;
+      }
+    } else {
+      uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+      if (nsec < A.sec_cap) {
+        R* sp = A.sec + ((uint64_t)gt * A.sec_cap + nsec) * 9;
+        sp[0] = rx; sp[1] = ry; sp[2] = rz;
+        sp[3] = uo.x; sp[4] = uo.y; sp[5] = uo.z;
+        sp[6] = E_out; sp[7] = wgt; sp[8] = R(0);
+        nsec++;
+      } else {
+        raise_err(A.st, ABX_ERR_CAPACITY, h);
+        atomicAdd(&A.st->sec_overflow, 1ull);
+      }
+    }
+  }
+  return FissionOut{rng, nsec};
+}
+
 // Transporter::collision + branching_collision + russian_roulette +
 // make_fission_neutrons + do_scatter (src/transporter.cpp:35-93, 269-347, 358-487),
 // MGNuclide::sample_scatter / sample_fission (src/mg_nuclide.cpp:442-461, 504-544)
-template <class R>
+template <class R, bool ISO>
 ABX_DEV void collide(const TransportArgs<R>& A, const Tables& T, const View<R>& V, const ProbT& P,
                      Lane<R>& L, Acc<R>& acc, bool converged, R kcol, bool& alive) {
   const MatT M = T.mats[L.mat];
@@ -374,39 +429,14 @@ ABX_DEV void collide(const TransportArgs<R>& A, const Tables& T, const View<R>& 
       if (L.w > R(0)) L.npos += (uint32_t)n_new;
       else L.nneg += (uint32_t)n_new;
     }
-    const R* chi = V.cdf + M.cdf_off + G * G + g * G;
-    for (int i = 0; i < n_new; i++) {
-      int ei = discrete<R>(L.rng, chi, G);
-      R E_out = group_mid(V, P, ei);
-      R mu = R(2) * canon<R>(L.rng) - R(1);
-      R c, s;
-      azimuth(canon<R>(L.rng), c, s);
-      V3<R> uo = rotate(L.u, mu, c, s);
-      if (canon<R>(L.rng) < P_delayed) (void)discrete<R>(L.rng, V.dgcdf + M.dg_off, M.ndg);
-      R wgt = L.w > R(0) ? R(1) : R(-1);
-      if (keig) {
-        uint64_t j = base + i;
-        if (j < A.site_cap) {
-          A.sites.x[j] = L.r.x; A.sites.y[j] = L.r.y; A.sites.z[j] = L.r.z;
-          A.sites.ux[j] = uo.x; A.sites.uy[j] = uo.y; A.sites.uz[j] = uo.z;
-          A.sites.E[j] = E_out; A.sites.w[j] = wgt;
-          A.sites.hist[j] = L.h; A.sites.dau[j] = L.dau;
-        }
-        L.dau++;
-      } else {
-        L.dau++;
-        uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
-        if (L.nsec < A.sec_cap) {
-          R* sp = A.sec + ((uint64_t)gt * A.sec_cap + L.nsec) * 9;
-          sp[0] = L.r.x; sp[1] = L.r.y; sp[2] = L.r.z;
-          sp[3] = uo.x; sp[4] = uo.y; sp[5] = uo.z;
-          sp[6] = E_out; sp[7] = wgt; sp[8] = R(0);
-          L.nsec++;
-        } else {
-          raise_err(A.st, ABX_ERR_CAPACITY, L.h);
-          atomicAdd(&A.st->sec_overflow, 1ull);
-        }
-      }
+    if (n_new > 0) {
+      const FissionOut o = fission_neutrons<R>(A, V.cdf + M.cdf_off + G * G + g * G, V.ebnd + P.eb_off,
+                                               V.dgcdf + M.dg_off, G, M.ndg, P_delayed, n_new, base, L.rng,
+                                               L.r.x, L.r.y, L.r.z, L.u.x, L.u.y, L.u.z, L.w > R(0), L.h, L.dau,
+                                               L.nsec, keig);
+      L.rng = o.rng;
+      L.dau += (uint32_t)n_new;
+      L.nsec = o.nsec;
     }
   }
   // implicit capture
@@ -427,7 +457,7 @@ ABX_DEV void collide(const TransportArgs<R>& A, const Tables& T, const View<R>& 
   if (alive) {
     int ei = discrete<R>(L.rng, V.cdf + M.cdf_off + g * G, G);
     R E_out = group_mid(V, P, ei);
-    R mu = sample_mu(T, V, M, g, ei, L.rng);
+    R mu = sample_mu<R, ISO>(T, V, M, g, ei, L.rng);
     R c, s;
     azimuth(canon<R>(L.rng), c, s);
     L.u = rotate(L.u, mu, c, s);

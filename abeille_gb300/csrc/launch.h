@@ -38,13 +38,17 @@ void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace
 void launch_sources(const SourceArgs& A, cudaStream_t s);
 int transport_regs_d(int tracking);
 
-// transport_mixed.cu
-void launch_transport_f(const TransportArgs<float>& A, int tracking, bool trace, int grid, int block,
+// transport_mixed.cu (+ transport_mixed_surface.cu); `iso`: every material
+// of the problem scatters isotropically
+void launch_transport_f(const TransportArgs<float>& A, int tracking, bool iso, bool trace, int grid, int block,
                         cudaStream_t s);
+void launch_transport_f_surface(const TransportArgs<float>& A, bool iso, int grid, int block, cudaStream_t s);
 int transport_regs_f(int tracking);
+int transport_regs_f_surface();
 
 // occupancy helpers
 int occupancy_d(int tracking, int block);
-int occupancy_f(int tracking, int block);
+int occupancy_f(int tracking, bool iso, int block);
+int occupancy_f_surface(bool iso, int block);
 
 }  // namespace abx

@@ -6,31 +6,31 @@
 
 namespace abx {
 
-template __global__ void transport_kernel<double, ABX_TRACK_DELTA>(const __grid_constant__ TransportArgs<double>);
-template __global__ void transport_kernel<double, ABX_TRACK_SURFACE>(const __grid_constant__ TransportArgs<double>);
+template __global__ void transport_kernel<double, ABX_TRACK_DELTA, false>(const __grid_constant__ TransportArgs<double>);
+template __global__ void transport_kernel<double, ABX_TRACK_SURFACE, false>(const __grid_constant__ TransportArgs<double>);
 
 void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace, int grid, int block,
                         cudaStream_t s) {
   if (tracking == ABX_TRACK_DELTA) {
-    transport_kernel<double, ABX_TRACK_DELTA><<<grid, block, 0, s>>>(A);
+    transport_kernel<double, ABX_TRACK_DELTA, false><<<grid, block, 0, s>>>(A);
   } else {
-    transport_kernel<double, ABX_TRACK_SURFACE><<<grid, block, 0, s>>>(A);
+    transport_kernel<double, ABX_TRACK_SURFACE, false><<<grid, block, 0, s>>>(A);
   }
 }
 
 int occupancy_d(int tracking, int block) {
   int nb = 0;
   if (tracking == ABX_TRACK_DELTA)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_DELTA>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_DELTA, false>, block, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_SURFACE>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_SURFACE, false>, block, 0);
   return nb;
 }
 
 int transport_regs_d(int tracking) {
   cudaFuncAttributes a;
-  if (tracking == ABX_TRACK_DELTA) cudaFuncGetAttributes(&a, transport_kernel<double, ABX_TRACK_DELTA>);
-  else cudaFuncGetAttributes(&a, transport_kernel<double, ABX_TRACK_SURFACE>);
+  if (tracking == ABX_TRACK_DELTA) cudaFuncGetAttributes(&a, transport_kernel<double, ABX_TRACK_DELTA, false>);
+  else cudaFuncGetAttributes(&a, transport_kernel<double, ABX_TRACK_SURFACE, false>);
   return a.numRegs;
 }
 

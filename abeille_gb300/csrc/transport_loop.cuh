@@ -117,7 +117,7 @@ ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& ac
 // Occupancy (measured on config 1 and config 2): FP32 delta tracking runs four
 // 256-thread blocks per SM (64 registers), FP32 surface tracking three (80
 // registers), FP64 two (128 registers).
-template <class R, int TRACK>
+template <class R, int TRACK, bool ISO>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK == ABX_TRACK_DELTA ? 4 : 3) : 2)
     transport_kernel(const __grid_constant__ TransportArgs<R> A) {
   const bool TRACE = A.trace != nullptr;
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK == ABX_TRACK_DELT
       bool alive = true;
       ncoll++;
       L.hcoll++;
-      collide(A, T, V, P, L, acc, converged, kcol, alive);
+      collide<R, ISO>(A, T, V, P, L, acc, converged, kcol, alive);
       if (sizeof(R) == 4 && !(m_abs(L.u.x) <= R(1) && m_abs(L.u.y) <= R(1) && m_abs(L.u.z) <= R(1))) {
         // mixed mode: a direction that is not finite cannot be tracked
         ABX_LOST();

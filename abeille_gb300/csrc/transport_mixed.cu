@@ -1,35 +1,39 @@
-// Mixed-precision translation unit: positions, directions, flight distances
-// and cross sections in FP32; scores, tallies and k in FP64.
+// Mixed-precision translation unit, delta tracking: positions, directions,
+// flight distances and cross sections in FP32; scores, tallies and k in FP64.
+// Each tracking mode has one instantiation for problems whose materials all
+// scatter isotropically and one general; the surface-tracking pair lives in
+// transport_mixed_surface.cu so the two compile in parallel.
 #include "transport_loop.cuh"
 #include "launch.h"
 
 namespace abx {
 
-template __global__ void transport_kernel<float, ABX_TRACK_DELTA>(const __grid_constant__ TransportArgs<float>);
-template __global__ void transport_kernel<float, ABX_TRACK_SURFACE>(const __grid_constant__ TransportArgs<float>);
+template __global__ void transport_kernel<float, ABX_TRACK_DELTA, false>(const __grid_constant__ TransportArgs<float>);
+template __global__ void transport_kernel<float, ABX_TRACK_DELTA, true>(const __grid_constant__ TransportArgs<float>);
 
-void launch_transport_f(const TransportArgs<float>& A, int tracking, bool trace, int grid, int block,
+void launch_transport_f(const TransportArgs<float>& A, int tracking, bool iso, bool trace, int grid, int block,
                         cudaStream_t s) {
-  if (tracking == ABX_TRACK_DELTA) {
-    transport_kernel<float, ABX_TRACK_DELTA><<<grid, block, 0, s>>>(A);
+  if (tracking != ABX_TRACK_DELTA) {
+    launch_transport_f_surface(A, iso, grid, block, s);
+  } else if (iso) {
+    transport_kernel<float, ABX_TRACK_DELTA, true><<<grid, block, 0, s>>>(A);
   } else {
-    transport_kernel<float, ABX_TRACK_SURFACE><<<grid, block, 0, s>>>(A);
+    transport_kernel<float, ABX_TRACK_DELTA, false><<<grid, block, 0, s>>>(A);
   }
 }
 
-int occupancy_f(int tracking, int block) {
+int occupancy_f(int tracking, bool iso, int block) {
+  if (tracking != ABX_TRACK_DELTA) return occupancy_f_surface(iso, block);
   int nb = 0;
-  if (tracking == ABX_TRACK_DELTA)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<float, ABX_TRACK_DELTA>, block, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<float, ABX_TRACK_SURFACE>, block, 0);
+  if (iso) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<float, ABX_TRACK_DELTA, true>, block, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<float, ABX_TRACK_DELTA, false>, block, 0);
   return nb;
 }
 
 int transport_regs_f(int tracking) {
   cudaFuncAttributes a;
-  if (tracking == ABX_TRACK_DELTA) cudaFuncGetAttributes(&a, transport_kernel<float, ABX_TRACK_DELTA>);
-  else cudaFuncGetAttributes(&a, transport_kernel<float, ABX_TRACK_SURFACE>);
+  if (tracking == ABX_TRACK_DELTA) cudaFuncGetAttributes(&a, transport_kernel<float, ABX_TRACK_DELTA, false>);
+  else return transport_regs_f_surface();
   return a.numRegs;
 }
 
