@@ -342,7 +342,7 @@ struct FissionOut {
 };
 
 template <class R>
-__device__ __noinline__ FissionOut fission_neutrons(const TransportArgs<R>& A, const R* chi, const R* ebnd,
+ABX_DEV FissionOut fission_neutrons_body(const TransportArgs<R>& A, const R* chi, const R* ebnd,
                                                     const R* dgcdf, int G, int ndg, R P_delayed, int n_new,
                                                     uint64_t base, uint64_t rng, R rx, R ry, R rz, R ux, R uy,
                                                     R uz, bool positive, uint32_t h, uint32_t dau, uint32_t nsec,
@@ -380,6 +380,30 @@ __device__ __noinline__ FissionOut fission_neutrons(const TransportArgs<R>& A, c
     }
   }
   return FissionOut{rng, nsec};
+}
+
+// Out of line in FP32 tracking (measured faster on config 1), inline in FP64.
+template <class R>
+__device__ __noinline__ FissionOut fission_neutrons_ool(const TransportArgs<R>& A, const R* chi, const R* ebnd,
+                                                        const R* dgcdf, int G, int ndg, R P_delayed, int n_new,
+                                                        uint64_t base, uint64_t rng, R rx, R ry, R rz, R ux,
+                                                        R uy, R uz, bool positive, uint32_t h, uint32_t dau,
+                                                        uint32_t nsec, bool keig) {
+  return fission_neutrons_body<R>(A, chi, ebnd, dgcdf, G, ndg, P_delayed, n_new, base, rng, rx, ry, rz, ux, uy, uz,
+                                  positive, h, dau, nsec, keig);
+}
+
+template <class R>
+ABX_DEV FissionOut fission_neutrons(const TransportArgs<R>& A, const R* chi, const R* ebnd, const R* dgcdf, int G,
+                                    int ndg, R P_delayed, int n_new, uint64_t base, uint64_t rng, R rx, R ry, R rz,
+                                    R ux, R uy, R uz, bool positive, uint32_t h, uint32_t dau, uint32_t nsec,
+                                    bool keig) {
+  if constexpr (sizeof(R) == 4)
+    return fission_neutrons_ool<R>(A, chi, ebnd, dgcdf, G, ndg, P_delayed, n_new, base, rng, rx, ry, rz, ux, uy, uz,
+                                   positive, h, dau, nsec, keig);
+  else
+    return fission_neutrons_body<R>(A, chi, ebnd, dgcdf, G, ndg, P_delayed, n_new, base, rng, rx, ry, rz, ux, uy,
+                                    uz, positive, h, dau, nsec, keig);
 }
 
 // Transporter::collision + branching_collision + russian_roulette +
