@@ -721,6 +721,14 @@ struct abx_context {
   size_t vcap[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   size_t tally_rv_cap = 0;  // capacity of tally_avg / tally_var, in bins
   Tables batch_tables{};
+  // captured generation step (one graph per bank parity)
+  bool use_graphs = true;
+  cudaGraphExec_t gen_exec[2] = {nullptr, nullptr};
+  cudaGraphNode_t gen_ev_node[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  cudaEvent_t gen_ev_ph[2] = {nullptr, nullptr};
+  size_t gen_cap = 0;
+  int gen_nignored = -1;
+  std::vector<const void*> gen_sig;  // buffers the captured launches point at
 };
 
 static void ctx_free(abx_ctx* c) {
@@ -739,6 +747,10 @@ static void ctx_free(abx_ctx* c) {
   for (void* p : ps)
     if (p) cudaFree(p);
   if (c->st_host) cudaFreeHost(c->st_host);
+  for (auto& e : c->gen_exec)
+    if (e) cudaGraphExecDestroy(e);
+  for (auto& e : c->gen_ev_ph)
+    if (e) cudaEventDestroy(e);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -1010,6 +1022,13 @@ __global__ void k_tally_record_batches(double* gen, double* avg, double* var, si
   }
 }
 
+// The same, with the generation's bookkeeping read on the device (for the
+// captured generation step): a generation is recorded when it is active
+// (DevState::converged, set by the previous k_gen_end), as active generation
+// number RunAcc::active + 1.
+__global__ void k_tally_record_dev(double* gen, double* avg, double* var, size_t n, const DevState* st,
+                                   const struct RunAcc* run);
+
 // MeshTally::record_generation + clear_generation (src/mesh_tally.cpp:121-152)
 __global__ void k_tally_record(double* gen, double* avg, double* var, size_t n, double mult, int rec,
                                double dg) {
@@ -1017,6 +1036,24 @@ __global__ void k_tally_record(double* gen, double* avg, double* var, size_t n, 
     if (rec) {
       double old_avg = avg[i];
       double val = gen[i] * mult;
+      double a = old_avg + (val - old_avg) / dg;
+      avg[i] = a;
+      double v = var[i];
+      v = v + (((val - old_avg) * (val - a) - (v)) / dg);
+      var[i] = v;
+    }
+    gen[i] = 0.;
+  }
+}
+
+__global__ void k_tally_record_dev(double* gen, double* avg, double* var, size_t n, const DevState* st,
+                                   const RunAcc* run) {
+  const int rec = st->converged;
+  const double dg = (double)(run->active + 1);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (rec) {
+      double old_avg = avg[i];
+      double val = gen[i];
       double a = old_avg + (val - old_avg) / dg;
       avg[i] = a;
       double v = var[i];
@@ -1671,6 +1708,101 @@ static int ensure_records(abx_ctx* c, int n) {
   return ABX_OK;
 }
 
+// One power-iteration generation on the stream (src/power_iterator.cpp:
+// 333-404): transport of bank `cur`, the site count scan, the next bank
+// (bank order, weights, ids, streams, entropy bins) into bank 1-cur, the
+// tally record and the end-of-generation statistics.  `device_book`: the
+// tally record reads its active flag and count on the device (captured
+// graphs); otherwise they come from the host (`conv`, `active`).
+static int generation_step(abx_ctx* c, bool mixed, int cur, size_t cap, int nignored, cudaEvent_t ev_t0,
+                           cudaEvent_t ev_t1, bool device_book, bool conv, int active) {
+  int rc;
+  k_step_begin<<<1, 1, 0, c->stream>>>(c->st, 0, 0., 0, 1);
+  CUDA_TRY(cudaEventRecord(ev_t0, c->stream));
+  if ((rc = launch_transport(c, mixed, cur, cap)) != ABX_OK) return rc;
+  CUDA_TRY(cudaEventRecord(ev_t1, c->stream));
+  launch_scan(c, cap);
+  if (mixed)
+    k_next_bank<float><<<grid_for(cap), 256, 0, c->stream>>>(c->sf.s, c->st, c->offsets, c->bf[cur].b,
+                                                             c->bf[1 - cur].b, c->D.T.probs, c->run, cap,
+                                                             c->ent_bins, c->ent_total);
+  else
+    k_next_bank<double><<<grid_for(cap), 256, 0, c->stream>>>(c->sd.s, c->st, c->offsets, c->bd[cur].b,
+                                                              c->bd[1 - cur].b, c->D.T.probs, c->run, cap,
+                                                              c->ent_bins, c->ent_total);
+  if (c->P.tally_bins) {
+    if (device_book)
+      k_tally_record_dev<<<grid_for((size_t)c->P.tally_bins), 256, 0, c->stream>>>(
+          c->tally_gen, c->tally_avg, c->tally_var, (size_t)c->P.tally_bins, c->st, c->run);
+    else
+      k_tally_record<<<grid_for((size_t)c->P.tally_bins), 256, 0, c->stream>>>(
+          c->tally_gen, c->tally_avg, c->tally_var, (size_t)c->P.tally_bins, 1.0, conv ? 1 : 0,
+          (double)std::max(active, 1));
+  }
+  k_gen_end<<<1, 1024, 0, c->stream>>>(c->st, c->run, c->D.T.probs, c->gen_rec, c->hist_cap, c->ent_bins,
+                                       c->ent_total, c->ent_nbins, cap, 1, nignored);
+  CUDA_TRY(cudaGetLastError());
+  return ABX_OK;
+}
+
+// Captures the generation step once per bank parity (the launches of a
+// generation never change between generations: every per-generation value
+// lives in device memory), so a generation is one graph launch.
+static int ensure_gen_graphs(abx_ctx* c, bool mixed, size_t cap, int nignored) {
+  // everything a captured launch points at; a reallocation forces a new capture
+  std::vector<const void*> sig = {c->bd[0].b.x, c->bd[1].b.x, c->bf[0].b.x, c->bf[1].b.x, c->sd.s.x, c->sf.s.x,
+                                  c->hist_count, c->offsets, c->block_sums, c->tally_gen, c->tally_avg,
+                                  c->tally_var, c->ent_bins, c->ent_total, c->sec, c->st, c->run, c->gen_rec,
+                                  c->D.T.probs, (const void*)(uintptr_t)c->grid, (const void*)(uintptr_t)c->block,
+                                  (const void*)(uintptr_t)mixed};
+  if (c->gen_exec[0] && c->gen_cap == cap && c->gen_nignored == nignored && sig == c->gen_sig) return ABX_OK;
+  for (auto& e : c->gen_exec)
+    if (e) cudaGraphExecDestroy(e);
+  c->gen_exec[0] = c->gen_exec[1] = nullptr;
+  for (auto& e : c->gen_ev_ph)
+    if (!e) CUDA_TRY(cudaEventCreate(&e));
+  for (int cur = 0; cur < 2; cur++) {
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = generation_step(c, mixed, cur, cap, nignored, c->gen_ev_ph[0], c->gen_ev_ph[1], true, false, 0);
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+    if (rc != ABX_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (ce != cudaSuccess) return fail(ABX_ERR_CUDA, "generation capture failed: %s", cudaGetErrorString(ce));
+    // the two event-record nodes, to point them at each generation's events
+    size_t nn = 0;
+    cudaGraphGetNodes(graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    cudaGraphGetNodes(graph, nodes.data(), &nn);
+    c->gen_ev_node[cur][0] = c->gen_ev_node[cur][1] = nullptr;
+    for (cudaGraphNode_t n : nodes) {
+      cudaGraphNodeType ty;
+      cudaGraphNodeGetType(n, &ty);
+      if (ty != cudaGraphNodeTypeEventRecord) continue;
+      cudaEvent_t e;
+      cudaGraphEventRecordNodeGetEvent(n, &e);
+      if (e == c->gen_ev_ph[0]) c->gen_ev_node[cur][0] = n;
+      if (e == c->gen_ev_ph[1]) c->gen_ev_node[cur][1] = n;
+    }
+    ce = cudaGraphInstantiate(&c->gen_exec[cur], graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess || !c->gen_ev_node[cur][0] || !c->gen_ev_node[cur][1])
+      return fail(ABX_ERR_CUDA, "generation graph instantiation failed");
+  }
+  c->gen_cap = cap;
+  c->gen_nignored = nignored;
+  c->gen_sig = sig;
+  return ABX_OK;
+}
+
+extern "C" int abx_set_graphs(abx_ctx* c, int enabled) {
+  if (!c) return fail(ABX_ERR_INVALID, "bad arguments");
+  c->use_graphs = enabled != 0;
+  return ABX_OK;
+}
+
 extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, abx_run_stats* stats,
                                           abx_gen_record* per_gen) {
   if (!c || ngen <= 0 || nignored < 0) return fail(ABX_ERR_INVALID, "bad arguments");
@@ -1714,32 +1846,26 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
   for (auto& e : evs) cudaEventCreate(&e);
   int cur = 0;
   int active_tally = 0;
+  const bool graphs = c->use_graphs && c->trace_nhist == 0;
+  if (graphs && (rc = ensure_gen_graphs(c, mixed, cap, nignored)) != ABX_OK) {
+    for (auto& e : evs) cudaEventDestroy(e);
+    return rc;
+  }
   for (int g = 1; g <= ngen; g++) {
     if (c->flush_bytes) CUDA_TRY(cudaMemsetAsync(c->flush, g & 0xff, c->flush_bytes, c->stream));
     cudaEventRecord(evs[4 * (g - 1)], c->stream);
-    k_step_begin<<<1, 1, 0, c->stream>>>(c->st, 0, 0., 0, 1);
-    cudaEventRecord(evs[4 * (g - 1) + 1], c->stream);
-    if ((rc = launch_transport(c, mixed, cur, cap)) != ABX_OK) break;
-    cudaEventRecord(evs[4 * (g - 1) + 2], c->stream);
-    launch_scan(c, cap);
-    if (mixed)
-      k_next_bank<float><<<grid_for(cap), 256, 0, c->stream>>>(c->sf.s, c->st, c->offsets, c->bf[cur].b,
-                                                               c->bf[1 - cur].b, c->D.T.probs, c->run, cap,
-                                                               c->ent_bins, c->ent_total);
-    else
-      k_next_bank<double><<<grid_for(cap), 256, 0, c->stream>>>(c->sd.s, c->st, c->offsets, c->bd[cur].b,
-                                                                c->bd[1 - cur].b, c->D.T.probs, c->run, cap,
-                                                                c->ent_bins, c->ent_total);
-    // tallies: record when this generation is active, always clear
     bool conv = (nignored == 0) || (g > nignored);
-    if (c->P.tally_bins) {
-      if (conv) active_tally++;
-      k_tally_record<<<grid_for((size_t)c->P.tally_bins), 256, 0, c->stream>>>(
-          c->tally_gen, c->tally_avg, c->tally_var, (size_t)c->P.tally_bins, 1.0, conv ? 1 : 0,
-          (double)std::max(active_tally, 1));
+    if (conv) active_tally++;
+    if (graphs) {
+      // the captured step, its transport bracketed by this generation's events
+      CUDA_TRY(cudaGraphExecEventRecordNodeSetEvent(c->gen_exec[cur], c->gen_ev_node[cur][0], evs[4 * (g - 1) + 1]));
+      CUDA_TRY(cudaGraphExecEventRecordNodeSetEvent(c->gen_exec[cur], c->gen_ev_node[cur][1], evs[4 * (g - 1) + 2]));
+      CUDA_TRY(cudaGraphLaunch(c->gen_exec[cur], c->stream));
+    } else {
+      if ((rc = generation_step(c, mixed, cur, cap, nignored, evs[4 * (g - 1) + 1], evs[4 * (g - 1) + 2], false,
+                                conv, active_tally)) != ABX_OK)
+        break;
     }
-    k_gen_end<<<1, 1024, 0, c->stream>>>(c->st, c->run, c->D.T.probs, c->gen_rec, c->hist_cap, c->ent_bins,
-                                         c->ent_total, c->ent_nbins, cap, 1, nignored);
     cudaEventRecord(evs[4 * (g - 1) + 3], c->stream);
     CUDA_TRY(cudaGetLastError());
     cur = 1 - cur;

@@ -100,6 +100,9 @@ class Engine:
         self._chk(self.lib.abx_entropy(self.ctx, sites.ctypes.data_as(C.POINTER(abi.Site)), sites.size, C.byref(h)))
         return h.value
 
+    def set_graphs(self, enabled):
+        self._chk(self.lib.abx_set_graphs(self.ctx, int(bool(enabled))))
+
     def run_power_iteration(self, ngenerations, nignored):
         st = abi.RunStats()
         k = np.zeros(ngenerations)

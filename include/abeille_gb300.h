@@ -488,6 +488,12 @@ int abx_get_trace(abx_ctx* ctx, abx_trace_rec* out, size_t capacity, size_t* n_o
 /* Device time of the most recent transport launch, in milliseconds. */
 int abx_last_transport_ms(abx_ctx* ctx, double* ms);
 
+/* Power iteration runs each generation as one launch of a captured CUDA graph
+ * (the same kernels, in the same order, as the direct launches; no reference
+ * counterpart).  On by default; 0 launches the kernels one by one.  Traced
+ * runs always launch directly. */
+int abx_set_graphs(abx_ctx* ctx, int enabled);
+
 /* Timing hygiene for benchmarks (no reference counterpart): before each
  * generation of abx_run_power_iteration[_ex], outside the generation's timed
  * events, write `bytes` of a private device buffer so that the L2 cache holds

@@ -249,3 +249,25 @@ def test_mixed_config2_tracks_like_fp64(tracking):
     assert l32 <= 1e-4 * h32, out
     assert abs(f32 / h32 - f64 / h64) <= 0.02 * f64 / h64, out
     assert abs(c32 / h32 - c64 / h64) <= 0.02 * c64 / h64, out
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_captured_generation_step_matches_direct_launches(precision):
+    """Power iteration with each generation as one CUDA-graph launch against the
+    same kernels launched one by one: collision counts identical, k, entropy and
+    tallies within 1e-11 relative (FP64 atomic additions in another order)."""
+    out = {}
+    for graphs in (False, True):
+        eng = Engine(decks.config0(nparticles=3000).build(precision=precision), 0)
+        eng.set_graphs(graphs)
+        st, recs = eng.run_power_iteration_records(12, 4)
+        out[graphs] = (st, recs, eng.tally(0))
+        eng.close()
+    (s0, r0, t0), (s1, r1, t1) = out[False], out[True]
+    assert [r["collisions"] for r in r0] == [r["collisions"] for r in r1]
+    assert [r["sites"] for r in r0] == [r["sites"] for r in r1]
+    assert np.allclose([r["kcol"] for r in r0], [r["kcol"] for r in r1], rtol=1e-11, atol=0)
+    assert np.allclose([r["entropy"] for r in r0], [r["entropy"] for r in r1], rtol=1e-11, atol=0)
+    assert t0["generations"] == t1["generations"] == 8
+    assert np.allclose(t0["avg"], t1["avg"], rtol=1e-10, atol=0)
+    assert abs(s0["kcol_avg"] - s1["kcol_avg"]) <= 1e-11 * s0["kcol_avg"]
