@@ -1717,10 +1717,11 @@ static int ensure_records(abx_ctx* c, int n) {
 static int generation_step(abx_ctx* c, bool mixed, int cur, size_t cap, int nignored, cudaEvent_t ev_t0,
                            cudaEvent_t ev_t1, bool device_book, bool conv, int active) {
   int rc;
+  // external records: under stream capture they become event-record nodes
   k_step_begin<<<1, 1, 0, c->stream>>>(c->st, 0, 0., 0, 1);
-  CUDA_TRY(cudaEventRecord(ev_t0, c->stream));
+  CUDA_TRY(cudaEventRecordWithFlags(ev_t0, c->stream, cudaEventRecordExternal));
   if ((rc = launch_transport(c, mixed, cur, cap)) != ABX_OK) return rc;
-  CUDA_TRY(cudaEventRecord(ev_t1, c->stream));
+  CUDA_TRY(cudaEventRecordWithFlags(ev_t1, c->stream, cudaEventRecordExternal));
   launch_scan(c, cap);
   if (mixed)
     k_next_bank<float><<<grid_for(cap), 256, 0, c->stream>>>(c->sf.s, c->st, c->offsets, c->bf[cur].b,
@@ -1786,10 +1787,13 @@ static int ensure_gen_graphs(abx_ctx* c, bool mixed, size_t cap, int nignored) {
       if (e == c->gen_ev_ph[0]) c->gen_ev_node[cur][0] = n;
       if (e == c->gen_ev_ph[1]) c->gen_ev_node[cur][1] = n;
     }
+    if (!c->gen_ev_node[cur][0] || !c->gen_ev_node[cur][1]) {
+      cudaGraphDestroy(graph);
+      return fail(ABX_ERR_CUDA, "generation graph: transport event nodes not found");
+    }
     ce = cudaGraphInstantiate(&c->gen_exec[cur], graph, 0);
     cudaGraphDestroy(graph);
-    if (ce != cudaSuccess || !c->gen_ev_node[cur][0] || !c->gen_ev_node[cur][1])
-      return fail(ABX_ERR_CUDA, "generation graph instantiation failed");
+    if (ce != cudaSuccess) return fail(ABX_ERR_CUDA, "generation graph instantiation failed: %s", cudaGetErrorString(ce));
   }
   c->gen_cap = cap;
   c->gen_nignored = nignored;
