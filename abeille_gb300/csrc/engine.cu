@@ -724,6 +724,7 @@ struct abx_context {
   // captured generation step (one graph per bank parity)
   bool use_graphs = true;
   cudaGraphExec_t gen_exec[2] = {nullptr, nullptr};
+  cudaGraph_t gen_graph[2] = {nullptr, nullptr};  // kept: exec updates name its nodes
   cudaGraphNode_t gen_ev_node[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   cudaEvent_t gen_ev_ph[2] = {nullptr, nullptr};
   size_t gen_cap = 0;
@@ -749,6 +750,8 @@ static void ctx_free(abx_ctx* c) {
   if (c->st_host) cudaFreeHost(c->st_host);
   for (auto& e : c->gen_exec)
     if (e) cudaGraphExecDestroy(e);
+  for (auto& g : c->gen_graph)
+    if (g) cudaGraphDestroy(g);
   for (auto& e : c->gen_ev_ph)
     if (e) cudaEventDestroy(e);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1759,7 +1762,10 @@ static int ensure_gen_graphs(abx_ctx* c, bool mixed, size_t cap, int nignored) {
   if (c->gen_exec[0] && c->gen_cap == cap && c->gen_nignored == nignored && sig == c->gen_sig) return ABX_OK;
   for (auto& e : c->gen_exec)
     if (e) cudaGraphExecDestroy(e);
+  for (auto& g : c->gen_graph)
+    if (g) cudaGraphDestroy(g);
   c->gen_exec[0] = c->gen_exec[1] = nullptr;
+  c->gen_graph[0] = c->gen_graph[1] = nullptr;
   for (auto& e : c->gen_ev_ph)
     if (!e) CUDA_TRY(cudaEventCreate(&e));
   for (int cur = 0; cur < 2; cur++) {
@@ -1792,7 +1798,7 @@ static int ensure_gen_graphs(abx_ctx* c, bool mixed, size_t cap, int nignored) {
       return fail(ABX_ERR_CUDA, "generation graph: transport event nodes not found");
     }
     ce = cudaGraphInstantiate(&c->gen_exec[cur], graph, 0);
-    cudaGraphDestroy(graph);
+    c->gen_graph[cur] = graph;
     if (ce != cudaSuccess) return fail(ABX_ERR_CUDA, "generation graph instantiation failed: %s", cudaGetErrorString(ce));
   }
   c->gen_cap = cap;
