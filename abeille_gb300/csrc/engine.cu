@@ -730,6 +730,7 @@ struct abx_context {
   size_t gen_cap = 0;
   int gen_nignored = -1;
   std::vector<const void*> gen_sig;  // buffers the captured launches point at
+  std::vector<cudaEvent_t> ev_pool;  // per-generation timing events
 };
 
 static void ctx_free(abx_ctx* c) {
@@ -754,6 +755,7 @@ static void ctx_free(abx_ctx* c) {
     if (g) cudaGraphDestroy(g);
   for (auto& e : c->gen_ev_ph)
     if (e) cudaEventDestroy(e);
+  for (auto& e : c->ev_pool) cudaEventDestroy(e);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -1720,11 +1722,13 @@ static int ensure_records(abx_ctx* c, int n) {
 static int generation_step(abx_ctx* c, bool mixed, int cur, size_t cap, int nignored, cudaEvent_t ev_t0,
                            cudaEvent_t ev_t1, bool device_book, bool conv, int active) {
   int rc;
-  // external records: under stream capture they become event-record nodes
+  // under stream capture (device_book) the records are external, so they
+  // become event-record nodes of the graph
+  const unsigned evf = device_book ? cudaEventRecordExternal : cudaEventRecordDefault;
   k_step_begin<<<1, 1, 0, c->stream>>>(c->st, 0, 0., 0, 1);
-  CUDA_TRY(cudaEventRecordWithFlags(ev_t0, c->stream, cudaEventRecordExternal));
+  CUDA_TRY(cudaEventRecordWithFlags(ev_t0, c->stream, evf));
   if ((rc = launch_transport(c, mixed, cur, cap)) != ABX_OK) return rc;
-  CUDA_TRY(cudaEventRecordWithFlags(ev_t1, c->stream, cudaEventRecordExternal));
+  CUDA_TRY(cudaEventRecordWithFlags(ev_t1, c->stream, evf));
   launch_scan(c, cap);
   if (mixed)
     k_next_bank<float><<<grid_for(cap), 256, 0, c->stream>>>(c->sf.s, c->st, c->offsets, c->bf[cur].b,
@@ -1758,7 +1762,8 @@ static int ensure_gen_graphs(abx_ctx* c, bool mixed, size_t cap, int nignored) {
                                   c->hist_count, c->offsets, c->block_sums, c->tally_gen, c->tally_avg,
                                   c->tally_var, c->ent_bins, c->ent_total, c->sec, c->st, c->run, c->gen_rec,
                                   c->D.T.probs, (const void*)(uintptr_t)c->grid, (const void*)(uintptr_t)c->block,
-                                  (const void*)(uintptr_t)mixed};
+                                  (const void*)(uintptr_t)mixed, (const void*)(uintptr_t)c->hist_cap,
+                                  (const void*)(uintptr_t)c->ent_nbins};
   if (c->gen_exec[0] && c->gen_cap == cap && c->gen_nignored == nignored && sig == c->gen_sig) return ABX_OK;
   for (auto& e : c->gen_exec)
     if (e) cudaGraphExecDestroy(e);
@@ -1852,15 +1857,18 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
   if ((rc = check_state(c)) != ABX_OK) return rc;
   k_step_begin<<<1, 1, 0, c->stream>>>(c->st, N, 1.0, nignored == 0 ? 1 : 0, 0);
   if ((rc = ensure_sec(c, mixed)) != ABX_OK) return rc;
-  std::vector<cudaEvent_t> evs(4 * (size_t)ngen);
-  for (auto& e : evs) cudaEventCreate(&e);
+  // the generation events come from the context's pool and live as long as
+  // the context: a captured graph's event nodes keep pointing at them
+  while (c->ev_pool.size() < 4 * (size_t)ngen) {
+    cudaEvent_t e;
+    CUDA_TRY(cudaEventCreate(&e));
+    c->ev_pool.push_back(e);
+  }
+  const std::vector<cudaEvent_t> evs(c->ev_pool.begin(), c->ev_pool.begin() + 4 * (size_t)ngen);
   int cur = 0;
   int active_tally = 0;
   const bool graphs = c->use_graphs && c->trace_nhist == 0;
-  if (graphs && (rc = ensure_gen_graphs(c, mixed, cap, nignored)) != ABX_OK) {
-    for (auto& e : evs) cudaEventDestroy(e);
-    return rc;
-  }
+  if (graphs && (rc = ensure_gen_graphs(c, mixed, cap, nignored)) != ABX_OK) return rc;
   for (int g = 1; g <= ngen; g++) {
     if (c->flush_bytes) CUDA_TRY(cudaMemsetAsync(c->flush, g & 0xff, c->flush_bytes, c->stream));
     cudaEventRecord(evs[4 * (g - 1)], c->stream);
@@ -1896,7 +1904,6 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
     recs[g].transport_ms = ts;
     tms += ts;
   }
-  for (auto& e : evs) cudaEventDestroy(e);
   if (rc) return rc;
   auto t1 = std::chrono::steady_clock::now();
   RunAcc ra;
