@@ -1430,6 +1430,71 @@ extern "C" int abx_transport(abx_ctx* c, const abx_particle* bank, size_t n, dou
   return ABX_OK;
 }
 
+// ------------------------------------------------------------- autotuner
+// Picks the transport launch shape (threads per block, resident blocks per
+// SM) by timing the problem's own first-generation bank: `n_probe` source
+// histories are sampled once, then transported once per candidate (the same
+// histories each time, so every candidate does identical work) and the
+// fastest shape is kept for the context.  Results do not depend on the shape.
+extern "C" int abx_autotune(abx_ctx* c, size_t n_probe, int* block_out, int* grid_out, double* best_ms) {
+  if (!c || n_probe == 0 || n_probe > 0xffffffffull) return fail(ABX_ERR_INVALID, "bad arguments");
+  if (c->prob0.src_count <= 0) return fail(ABX_ERR_INVALID, "problem has no sources");
+  cudaSetDevice(c->device);
+  const bool mixed = mixed_of(c);
+  const bool keig = c->prob0.mode == ABX_MODE_K_EIGENVALUE;
+  int rc;
+  const size_t scap = keig ? 3 * n_probe + 4096 : 1;
+  if ((rc = ensure_banks(c, n_probe, mixed, false)) != ABX_OK) return rc;
+  if ((rc = ensure_sites(c, scap, mixed)) != ABX_OK) return rc;
+  CUDA_TRY(cudaMemsetAsync(c->st, 0, sizeof(DevState), c->stream));
+  SourceArgs S{};
+  S.T = c->D.T;
+  S.prob = 0;
+  S.first_hid = 0;
+  S.n = n_probe;
+  BankT<double>& b0 = c->bd[0].b;
+  S.x = b0.x; S.y = b0.y; S.z = b0.z; S.ux = b0.ux; S.uy = b0.uy; S.uz = b0.uz; S.E = b0.E; S.w = b0.w;
+  S.w2 = b0.w2; S.rng = b0.rng; S.hid = b0.hid; S.fam = b0.fam; S.probv = nullptr; S.out_off = 0; S.st = c->st;
+  launch_sources(S, c->stream);
+  if (mixed) k_bank_d2f<<<grid_for(n_probe), 256, 0, c->stream>>>(b0, c->bf[0].b, 0, n_probe);
+  if ((rc = check_state(c)) != ABX_OK) return rc;
+  const int block0 = c->block, grid0 = c->grid;
+  int best_block = block0, best_grid = grid0;
+  float best = -1.f;
+  for (int block : {128, 256}) {
+    const int occ = mixed ? occupancy_f(c->prob0.tracking, c->all_iso, block) : occupancy_d(c->prob0.tracking, block);
+    for (int per_sm = 1; per_sm <= occ; per_sm++) {
+      c->block = block;
+      c->grid = c->nsm * per_sm;
+      if ((rc = ensure_sec(c, mixed)) != ABX_OK) break;
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; rep++) {  // the first run warms the caches
+        k_step_begin<<<1, 1, 0, c->stream>>>(c->st, n_probe, 1.0, 0, 0);
+        CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+        if ((rc = launch_transport(c, mixed, 0, keig ? scap : 0)) != ABX_OK) break;
+        CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+        if ((rc = check_state(c)) != ABX_OK) break;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+      }
+      if (rc) break;
+      if (best < 0.f || ms < best) {
+        best = ms;
+        best_block = block;
+        best_grid = c->grid;
+      }
+    }
+    if (rc) break;
+  }
+  c->block = rc ? block0 : best_block;
+  c->grid = rc ? grid0 : best_grid;
+  if (rc) return rc;
+  if ((rc = ensure_sec(c, mixed)) != ABX_OK) return rc;
+  if (block_out) *block_out = c->block;
+  if (grid_out) *grid_out = c->grid;
+  if (best_ms) *best_ms = best;
+  return ABX_OK;
+}
+
 // ------------------------------------------------- transport, no allocation
 // abx_transport_noalloc: the transport step for callers that must not
 // allocate device memory while they run -- hosts that route every device

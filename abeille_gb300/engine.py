@@ -100,6 +100,13 @@ class Engine:
         self._chk(self.lib.abx_entropy(self.ctx, sites.ctypes.data_as(C.POINTER(abi.Site)), sites.size, C.byref(h)))
         return h.value
 
+    def autotune(self, n_probe):
+        """Time the transport launch shapes on `n_probe` source histories and keep
+        the fastest; returns (threads per block, blocks, best ms)."""
+        b, g, ms = C.c_int(), C.c_int(), C.c_double()
+        self._chk(self.lib.abx_autotune(self.ctx, n_probe, C.byref(b), C.byref(g), C.byref(ms)))
+        return b.value, g.value, ms.value
+
     def set_graphs(self, enabled):
         self._chk(self.lib.abx_set_graphs(self.ctx, int(bool(enabled))))
 

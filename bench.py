@@ -195,6 +195,8 @@ def main():
     ap.add_argument("--rates", default="200,1000,5000", help="config 4: Poisson arrival rates, requests/s")
     ap.add_argument("--duration", type=float, default=3.0, help="config 4: seconds of arrivals per rate")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="config 4: HBM admission budget")
+    ap.add_argument("--autotune", type=int, default=0,
+                    help="configs 0-2: tune the transport launch shape on this many source histories first")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -215,6 +217,9 @@ def main():
     builder.seed = builder.seed + 7919 * rank  # independent replica per rank
     eng = Engine(builder.build(precision=args.precision), local)
 
+    shape = None
+    if args.autotune:
+        shape = eng.autotune(args.autotune)
     # L2 flush between generations, outside each generation's timed events
     from abeille_gb300 import abi as _abi
     _abi.check(eng.lib.abx_set_l2_flush(eng.ctx, L2_FLUSH_BYTES), eng.lib)
@@ -275,7 +280,9 @@ def main():
         "config": {"workload": f"config{args.config}", "histories_per_generation": npart,
                    "tracking": builder.tracking, "precision": args.precision,
                    "l2": f"flushed: {L2_FLUSH_BYTES >> 20} MiB written before each generation, outside its "
-                   "timed events", "parallelism": f"replicas{world}"},
+                   "timed events", "parallelism": f"replicas{world}",
+                   "launch": {"autotuned": bool(shape), "block": shape[0] if shape else None,
+                              "grid": shape[1] if shape else None}},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": KERNELS_PER_GEN * args.steps,
         "clocks": clk.summary(),

@@ -271,3 +271,19 @@ def test_captured_generation_step_matches_direct_launches(precision):
     assert t0["generations"] == t1["generations"] == 8
     assert np.allclose(t0["avg"], t1["avg"], rtol=1e-10, atol=0)
     assert abs(s0["kcol_avg"] - s1["kcol_avg"]) <= 1e-11 * s0["kcol_avg"]
+
+
+def test_autotuned_launch_shape_gives_the_same_results():
+    b = decks.config0(nparticles=4096)
+    eng, ora, _ = pair(b)
+    bank = ora.sample_sources(0, 4096)
+    s0, c0 = eng.transport(bank, 1.1, True)
+    block, grid, ms = eng.autotune(20000)
+    assert block in (128, 256) and grid % 152 == 0 or grid > 0
+    assert ms > 0
+    s1, c1 = eng.transport(bank, 1.1, True)
+    assert np.array_equal(s0["parent_history_id"], s1["parent_history_id"])
+    assert np.array_equal(s0["parent_daughter_id"], s1["parent_daughter_id"])
+    assert close(s0["r"], s1["r"], atol=0) and c0["collisions"] == c1["collisions"]
+    assert abs(c0["k_col"] - c1["k_col"]) <= RTOL * abs(c0["k_col"])
+    eng.close()
