@@ -195,8 +195,8 @@ def main():
     ap.add_argument("--rates", default="200,1000,5000", help="config 4: Poisson arrival rates, requests/s")
     ap.add_argument("--duration", type=float, default=3.0, help="config 4: seconds of arrivals per rate")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="config 4: HBM admission budget")
-    ap.add_argument("--autotune", type=int, default=0,
-                    help="configs 0-2: tune the transport launch shape on this many source histories first")
+    ap.add_argument("--autotune", type=int, default=200000,
+                    help="configs 0-2: tune the transport launch shape on this many source histories first (0: off)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
