@@ -216,6 +216,92 @@ class ProblemBuilder:
         s.energy_value = float(energy)
         self.sources.append(s)
 
+    # ------------------------------------------------------------ deck output
+    def to_deck(self, ngenerations=None, nignored=None):
+        """The problem as a reference-format deck dictionary (write it with
+        deck.dump_yaml), so the reference can run the same problem."""
+        G = self.G
+        inv = {v: k for k, v in abi.SURF.items()}
+        keys = {"xplane": ["x0"], "yplane": ["y0"], "zplane": ["z0"], "plane": ["A", "B", "C", "D"],
+                "xcylinder": ["y0", "z0", "r"], "ycylinder": ["x0", "z0", "r"], "zcylinder": ["x0", "y0", "r"],
+                "sphere": ["x0", "y0", "z0", "r"]}
+        mats = []
+        for m in self.materials:
+            d = m["data"]
+            if m["n_delayed"]:
+                raise ValueError("delayed-neutron data is not written to decks")
+            o = 0
+            tot, ab, fi, nup, nud = (d[o + k * G:o + (k + 1) * G] for k in range(5))
+            o = 5 * G
+            chi = d[o:o + G * G].reshape(G, G)
+            sc = d[o + G * G:o + 2 * G * G].reshape(G, G)
+            e = {"id": m["id"], "total": tot.tolist(), "absorption": ab.tolist(), "scatter": sc.tolist()}
+            if m["fissile"]:
+                e["fission"] = fi.tolist()
+                e["nu"] = (nup + nud).tolist()
+                e["chi"] = [chi[0].tolist()] if np.all(chi == chi[0]) else chi.tolist()
+            mom = d[o + 2 * G * G:o + 2 * G * G + m["n_legendre"] * G * G].reshape(m["n_legendre"], G, G)
+            for l in range(m["n_legendre"]):
+                e[f"P{l + 1}"] = mom[l].tolist()
+            mats.append(e)
+        surfs = []
+        for sf in self.surfaces:
+            e = {"type": sf["kind"]}
+            e.update({k: v for k, v in zip(keys[sf["kind"]], sf["c"])})
+            e["boundary"] = sf["bc"]
+            e["id"] = sf["id"]
+            surfs.append(e)
+        cells = []
+        for c in self.cells:
+            e = {"region": c["region"]}
+            if c["material"] is not None:
+                e["material"] = c["material"]
+            else:
+                e["universe"] = c["universe"]
+            e["id"] = c["id"]
+            cells.append(e)
+        univs = []
+        for uid in self.universe_decl:
+            u = self.universes[uid]
+            if u["kind"] == "cells":
+                univs.append({"cells": u["cells"], "id": uid})
+            else:
+                e = {"id": uid, "type": "rectlinear", "shape": u["shape"], "pitch": u["pitch"],
+                     "origin": u["origin"], "universes": u["tiles"]}
+                if u["outer"] != -1:
+                    e["outer"] = u["outer"]
+                univs.append(e)
+        srcs = []
+        for so in self.sources:
+            sp = ({"type": "point", "position": [so.low[a] for a in range(3)]} if so.spatial == abi.SPATIAL["point"]
+                  else {"type": "box", "low": [so.low[a] for a in range(3)], "hi": [so.hi[a] for a in range(3)]})
+            if so.fissile_only:
+                sp["fissile-only"] = True
+            dr = ({"type": "isotropic"} if so.direction == abi.DIRECTION["isotropic"]
+                  else {"type": "mono-directional", "direction": [so.dir[a] for a in range(3)]})
+            srcs.append({"spatial": sp, "direction": dr, "energy": {"type": "mono-energetic",
+                                                                    "energy": so.energy_value},
+                         "weight": so.weight})
+        est = {v: k for k, v in abi.EST.items()}
+        qty = {v: k for k, v in abi.QUANTITY.items()}
+        tallies = [{"shape": t["shape"], "low": t["low"], "hi": t["hi"], "estimator": est[t["est"]],
+                    "quantity": qty[t["q"]], "energy-bounds": np.asarray(t["eb"]).tolist()} for t in self.tallies]
+        settings = {"nparticles": int(self.nparticles), "ngroups": G, "transport": self.tracking,
+                    "simulation": self.mode, "energy-mode": "multi-group",
+                    "energy-bounds": self.energy_bounds.tolist(), "seed": int(self.seed), "stride": int(self.stride)}
+        if ngenerations is not None:
+            settings["ngenerations"] = int(ngenerations)
+        if nignored is not None:
+            settings["nignored"] = int(nignored)
+        deck = {"materials": mats, "surfaces": surfs, "cells": cells, "universes": univs,
+                "root-universe": self.root, "sources": srcs}
+        if tallies:
+            deck["tallies"] = tallies
+        if self.entropy:
+            deck["entropy"] = dict(self.entropy)
+        deck["settings"] = settings
+        return deck
+
     # ------------------------------------------------------------- flattening
     def universe_order(self):
         """geometry::universes order of the reference parser."""
