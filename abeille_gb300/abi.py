@@ -27,7 +27,7 @@ QUANTITY = {"flux": 0, "elastic": 1, "absorption": 2, "fission": 3, "total": 4}
 SPATIAL = {"point": 0, "box": 1}
 DIRECTION = {"isotropic": 0, "mono-directional": 1}
 MODE = {"k-eigenvalue": 0, "fixed-source": 1}
-TRACKING = {"delta-tracking": 0, "surface-tracking": 1}
+TRACKING = {"delta-tracking": 0, "surface-tracking": 1, "implicit-leakage-delta-tracking": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
 
 

@@ -1,12 +1,13 @@
 """In-tree build of the CUDA engine (sm_103a) into abeille_gb300/_lib/.
 
-Five translation units are compiled in parallel with nvcc and linked into one
+Six translation units are compiled in parallel with nvcc and linked into one
 shared library exposing the C-ABI of include/abeille_gb300.h:
 
   engine.cu                   host side + bookkeeping kernels     --fmad=false
   transport_fp64.cu           FP64 parity transport kernels        --fmad=false
   transport_mixed.cu          FP32-tracking kernels, delta tracking
   transport_mixed_surface.cu  FP32-tracking kernels, surface tracking
+  transport_mixed_ildt.cu     FP32-tracking kernels, implicit-leakage delta tracking
   server.cpp                  request loop (host scheduler thread)
 
 Host code is compiled with -ffp-contract=off so derived tables round the same
@@ -32,6 +33,7 @@ UNITS = [
     ("transport_fp64.cu", ["--fmad=false"]),
     ("transport_mixed.cu", []),
     ("transport_mixed_surface.cu", []),
+    ("transport_mixed_ildt.cu", []),
     ("server.cpp", []),
 ]
 

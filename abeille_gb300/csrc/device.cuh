@@ -46,6 +46,8 @@ template <> struct Tol<float> {
 
 ABX_DEV double m_log(double x) { return log(x); }
 ABX_DEV float m_log(float x) { return logf(x); }
+ABX_DEV double m_exp(double x) { return exp(x); }
+ABX_DEV float m_exp(float x) { return expf(x); }
 ABX_DEV double m_sqrt(double x) { return sqrt(x); }
 ABX_DEV float m_sqrt(float x) { return sqrtf(x); }
 ABX_DEV double m_floor(double x) { return floor(x); }

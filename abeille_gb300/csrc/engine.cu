@@ -150,7 +150,7 @@ static int append_problem(Pools& P, const abx_problem* pr) {
   if (G < 1 || G > 1024) return fail(ABX_ERR_INVALID, "ngroups %d out of range", G);
   if (s.mode != ABX_MODE_K_EIGENVALUE && s.mode != ABX_MODE_FIXED_SOURCE)
     return fail(ABX_ERR_UNSUPPORTED, "simulation mode %d is outside the multigroup transport path", s.mode);
-  if (s.tracking != ABX_TRACK_DELTA && s.tracking != ABX_TRACK_SURFACE)
+  if (s.tracking != ABX_TRACK_DELTA && s.tracking != ABX_TRACK_SURFACE && s.tracking != ABX_TRACK_IMPLICIT_LEAKAGE)
     return fail(ABX_ERR_UNSUPPORTED, "tracking mode %d not supported", s.tracking);
   if (!pr->energy_bounds) return fail(ABX_ERR_INVALID, "no energy bounds");
   for (int g = 0; g < G; g++)

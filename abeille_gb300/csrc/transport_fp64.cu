@@ -8,11 +8,15 @@ namespace abx {
 
 template __global__ void transport_kernel<double, ABX_TRACK_DELTA, false>(const __grid_constant__ TransportArgs<double>);
 template __global__ void transport_kernel<double, ABX_TRACK_SURFACE, false>(const __grid_constant__ TransportArgs<double>);
+template __global__ void transport_kernel<double, ABX_TRACK_IMPLICIT_LEAKAGE, false>(
+    const __grid_constant__ TransportArgs<double>);
 
 void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace, int grid, int block,
                         cudaStream_t s) {
   if (tracking == ABX_TRACK_DELTA) {
     transport_kernel<double, ABX_TRACK_DELTA, false><<<grid, block, 0, s>>>(A);
+  } else if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE) {
+    transport_kernel<double, ABX_TRACK_IMPLICIT_LEAKAGE, false><<<grid, block, 0, s>>>(A);
   } else {
     transport_kernel<double, ABX_TRACK_SURFACE, false><<<grid, block, 0, s>>>(A);
   }
@@ -22,6 +26,9 @@ int occupancy_d(int tracking, int block) {
   int nb = 0;
   if (tracking == ABX_TRACK_DELTA)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_DELTA, false>, block, 0);
+  else if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_IMPLICIT_LEAKAGE, false>,
+                                                  block, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_SURFACE, false>, block, 0);
   return nb;

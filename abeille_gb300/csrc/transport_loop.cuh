@@ -114,11 +114,11 @@ ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& ac
   }
 }
 
-// Occupancy (measured on config 1 and config 2): FP32 delta tracking runs four
-// 256-thread blocks per SM (64 registers), FP32 surface tracking three (80
-// registers), FP64 two (128 registers).
+// Occupancy (measured on config 1 and config 2): FP32 delta tracking (and
+// implicit-leakage delta tracking) runs four 256-thread blocks per SM (64
+// registers), FP32 surface tracking three (80 registers), FP64 two (128).
 template <class R, int TRACK, bool ISO>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK == ABX_TRACK_DELTA ? 4 : 3) : 2)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURFACE ? 4 : 3) : 2)
     transport_kernel(const __grid_constant__ TransportArgs<R> A) {
   const bool TRACE = A.trace != nullptr;
   const Tables& T = A.T;
@@ -197,7 +197,65 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK == ABX_TRACK_DELT
       const ProbT& P = T.probs[L.pid];
       L.events++;
       nflight++;
-      if (TRACK == ABX_TRACK_DELTA) {
+      if (TRACK == ABX_TRACK_IMPLICIT_LEAKAGE) {
+        // ImplicitLeakageDeltaTracker::transport
+        // (src/implicit_leakage_delta_tracker.cpp:104-214): the nearest
+        // boundary condition before every flight; towards a vacuum boundary
+        // the weight that would leak is scored at once and the flight is
+        // sampled within the boundary distance.
+        const R Emaj = V.maj[P.maj_off + L.g];
+        const Bound<R> b = trk_bc_ool<R>(T, P, k);
+        if (b.btype == ABX_BC_VACUUM) {
+          const R P_leak = m_exp(-Emaj * b.dist);
+          const R P_no_leak = R(1) - P_leak;
+          const R wgt_leak = L.w * P_leak, wgt2_leak = L.w2 * P_leak;
+          const R wgt_coll = L.w * P_no_leak, wgt2_coll = L.w2 * P_no_leak;
+          acc.hleak += wgt_leak;
+          const V3<R> dl = sub(add(L.r, scl(L.u, b.dist)), L.rb);
+          acc.hmig += dot(scl(dl, wgt_leak), dl);
+          dcol = -m_log(R(1) - P_no_leak * canon<R>(L.rng)) / Emaj;
+          if (converged && P.has_tle) {
+            L.w = wgt_leak;
+            L.w2 = wgt2_leak;
+            score_flight(T, V, P, L, b.dist);
+          }
+          L.w = wgt_coll;
+          L.w2 = wgt2_coll;
+          if (converged && P.has_tle) score_flight(T, V, P, L, dcol);
+        } else {
+          dcol = Emaj == R(0) ? Tol<R>::INF : -m_log(R(1) - canon<R>(L.rng)) / Emaj;
+          if (converged && P.has_tle) score_flight(T, V, P, L, dcol < b.dist ? dcol : b.dist);
+        }
+        if (b.dist < dcol || m_abs(b.dist - dcol) < Tol<R>::BTOL) {
+          if (b.btype == ABX_BC_VACUUM) {
+            acc.hleak += L.w;
+            const V3<R> dl = sub(add(L.r, scl(L.u, b.dist)), L.rb);
+            acc.hmig += dot(scl(dl, L.w), dl);
+            if (TRACE) trace_rec(A, L, 2, k.cell);
+            ph = PH_DEAD;
+          } else if (b.btype == ABX_BC_REFLECTIVE) {
+            reflect_move(V, k, L, b);
+            dmode = 1;
+            after = PH_REFL;
+            ph = PH_WAIT;
+          } else if (sizeof(R) == 8) {
+            ABX_FAIL(ABX_ERR_LOST_PARTICLE);
+          } else {
+            ABX_LOST();
+            ph = PH_DEAD;
+          }
+        } else {
+          trk_move(k, dcol);
+          const int r = trk_check(T, V, k, dui, dfr);
+          if (r) {
+            dmode = r;
+            after = PH_MOVED;
+            ph = PH_WAIT;
+          } else {
+            ph = PH_MOVED;
+          }
+        }
+      } else if (TRACK == ABX_TRACK_DELTA) {
         // DeltaTracker::transport (src/delta_tracker.cpp:105-118)
         const R Emaj = V.maj[P.maj_off + L.g];
         dcol = Emaj == R(0) ? Tol<R>::INF : -m_log(R(1) - canon<R>(L.rng)) / Emaj;
@@ -326,16 +384,22 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK == ABX_TRACK_DELT
 
     // ----------------------------------------------------------------- moved
     if (ph == PH_MOVED) {
-      if (k.cell < 0) {
+      if (k.cell < 0 && TRACK == ABX_TRACK_DELTA) {
         // flew out of the geometry: back to the last position, find the
         // boundary condition (src/delta_tracker.cpp:120-127)
         trk_set_r(k, L.r);
         dmode = 1;
         after = PH_LOST;
         ph = PH_WAIT;
+      } else if (k.cell < 0) {
+        // implicit leakage: flights end inside the boundary conditions
+        if (sizeof(R) == 8) ABX_FAIL(ABX_ERR_LOST_PARTICLE) else {
+          ABX_LOST();
+          ph = PH_DEAD;
+        }
       } else {
         const ProbT& P = T.probs[L.pid];
-        if (converged && P.has_tle) score_flight(T, V, P, L, dcol);
+        if (TRACK == ABX_TRACK_DELTA && converged && P.has_tle) score_flight(T, V, P, L, dcol);
         L.r = add(L.r, scl(L.u, dcol));
         L.mat = T.cells[k.cell].fill;
         const MatT& M = T.mats[L.mat];

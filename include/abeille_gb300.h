@@ -178,7 +178,10 @@ typedef struct abx_source {
 
 /* ------------------------------------------------------------- settings */
 enum { ABX_MODE_K_EIGENVALUE = 0, ABX_MODE_FIXED_SOURCE = 1 };
-enum { ABX_TRACK_DELTA = 0, ABX_TRACK_SURFACE = 1 };
+/* Transporters: DeltaTracker (src/delta_tracker.cpp), SurfaceTracker
+ * (src/surface_tracker.cpp), ImplicitLeakageDeltaTracker
+ * (src/implicit_leakage_delta_tracker.cpp). */
+enum { ABX_TRACK_DELTA = 0, ABX_TRACK_SURFACE = 1, ABX_TRACK_IMPLICIT_LEAKAGE = 2 };
 /* ABX_PREC_FP64: every operation in double, reference draw order, no FMA
  *   contraction: reproduces the reference per history.
  * ABX_PREC_MIXED: positions, directions, flight distances and cross sections

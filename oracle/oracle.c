@@ -1140,11 +1140,81 @@ static int run_history(oracle_ctx* ctx, const abx_particle* in, uint32_t h, doub
   }
   int mat = t.cell >= 0 ? ctx->cell[t.cell].fill : -1;
   const int delta = ctx->set.tracking == ABX_TRACK_DELTA;
+  const int ildt = ctx->set.tracking == ABX_TRACK_IMPLICIT_LEAKAGE;
   int rc = ABX_OK;
   while (p.alive) {
     int had_collision = 0;
     int g = group_of(ctx, p.s.E);
-    if (delta) {
+    if (ildt) {
+      /* ImplicitLeakageDeltaTracker::transport
+       * (src/implicit_leakage_delta_tracker.cpp:104-214): the nearest
+       * boundary condition before every flight; towards a vacuum boundary the
+       * weight that would leak is scored as leakage at once and the flight is
+       * sampled within the boundary distance. */
+      double Emaj = ctx->maj[g];
+      Boundary bound = trk_get_bc(ctx, &t);
+      if (ctx->err) return ctx->err;
+      double d_coll;
+      sc->flights++;
+      if (bound.btype == ABX_BC_VACUUM) {
+        const double P_leak = exp(-Emaj * bound.distance);
+        const double P_no_leak = 1. - P_leak;
+        const double wgt_leak = p.s.w * P_leak, wgt2_leak = p.s.w2 * P_leak;
+        const double wgt_coll = p.s.w * P_no_leak, wgt2_coll = p.s.w2 * P_no_leak;
+        sc->leak += wgt_leak;
+        V3 r_leak = vadd(p.s.r, vscale(p.s.u, bound.distance));
+        V3 dl = vsub(r_leak, p.r_birth);
+        sc->mig += vdot(vscale(dl, wgt_leak), dl);
+        d_coll = -log(1. - P_no_leak * oracle_canonical(&p.rng)) / Emaj;
+        p.s.w = wgt_leak;
+        p.s.w2 = wgt2_leak;
+        if (converged) score_flight(ctx, &p, bound.distance, mat);
+        p.s.w = wgt_coll;
+        p.s.w2 = wgt2_coll;
+        if (converged) score_flight(ctx, &p, d_coll, mat);
+      } else {
+        d_coll = oracle_exponential(&p.rng, Emaj);
+        if (converged) score_flight(ctx, &p, d_coll < bound.distance ? d_coll : bound.distance, mat);
+      }
+      if (bound.distance < d_coll || fabs(bound.distance - d_coll) < BOUNDRY_TOL_) {
+        if (bound.btype == ABX_BC_VACUUM) {
+          p.alive = 0;
+          sc->leak += p.s.w;
+          V3 r_leak = vadd(p.s.r, vscale(p.s.u, bound.distance));
+          V3 dl = vsub(r_leak, p.r_birth);
+          sc->mig += vdot(vscale(dl, p.s.w), dl);
+          trace(ctx, tb, h, 2, &p, t.cell);
+        } else if (bound.btype == ABX_BC_REFLECTIVE) {
+          do_reflection(ctx, &t, &p, bound);
+          if (ctx->err) return ctx->err;
+          if (t.cell < 0) {
+            set_err("particle %llu lost after reflection", (unsigned long long)p.hid);
+            return ABX_ERR_LOST_PARTICLE;
+          }
+          trace(ctx, tb, h, 3, &p, t.cell);
+        } else {
+          set_err("boundary crossing without a boundary condition");
+          return ABX_ERR_LOST_PARTICLE;
+        }
+      } else {
+        p.s.r = vadd(p.s.r, vscale(p.s.u, d_coll));
+        trk_move(&t, d_coll);
+        trk_get_current(ctx, &t);
+        if (ctx->err) return ctx->err;
+        if (t.cell < 0) {
+          set_err("particle %llu lost after a flight of %g cm", (unsigned long long)p.hid, d_coll);
+          return ABX_ERR_LOST_PARTICLE;
+        }
+        mat = ctx->cell[t.cell].fill;
+        double Et = MAT_AT(ctx->Et, mat, g);
+        if (Et - Emaj > 1.E-10) {
+          set_err("Total cross section excedeed majorant: Et = %g, Emaj = %g", Et, Emaj);
+          return ABX_ERR_MAJORANT;
+        }
+        if (oracle_canonical(&p.rng) < (Et / Emaj)) had_collision = 1;
+        trace(ctx, tb, h, had_collision ? 1 : 0, &p, t.cell);
+      }
+    } else if (delta) {
       double Emaj = ctx->maj[g];
       double d_coll = oracle_exponential(&p.rng, Emaj);
       Boundary bound = {INF_, -1, ABX_BC_NORMAL, 0};

@@ -69,7 +69,8 @@ def test_event_traces_match_per_history(cfg, tracking):
 
 
 @pytest.mark.parametrize("cfg,tracking", [(0, "delta-tracking"), (1, "delta-tracking"), (2, "surface-tracking"),
-                                          (2, "delta-tracking")])
+                                          (2, "delta-tracking"), (1, "implicit-leakage-delta-tracking"),
+                                          (2, "implicit-leakage-delta-tracking")])
 def test_transport_step_matches(cfg, tracking):
     n = 4096 if cfg != 2 else 1024
     b = decks.CONFIGS[cfg](nparticles=n, tracking=tracking)
@@ -134,11 +135,28 @@ def test_reference_decks_trace_parity(name):
     compare_traces(eng.get_trace(), ora.get_trace())
 
 
-@pytest.mark.parametrize("name,precision", [("PUa-1-0-IN", "fp64"), ("PUa-1-0-IN", "mixed"),
-                                            ("PUb-1-0-SL", "mixed")])
-def test_reference_known_answers_on_gpu(name, precision):
+@pytest.mark.parametrize("name,tracking", [("PUa-1-0-SL", "implicit-leakage-delta-tracking"),
+                                           ("UD2O-2-1-SL", "implicit-leakage-delta-tracking"),
+                                           ("Ua-1-1-CY", "implicit-leakage-delta-tracking")])
+def test_implicit_leakage_traces_match(name, tracking):
+    b = decks.from_reference_deck(DECKS[name], nparticles=256, tracking=tracking)
+    eng, ora, _ = pair(b)
+    bank = ora.sample_sources(0, 256)
+    eng.set_trace(128, 1 << 20)
+    ora.set_trace(128, 1 << 20)
+    sg, cg = eng.transport(bank, 1.0, True)
+    sc, cc = ora.transport(bank, 1.0, True)
+    compare_traces(eng.get_trace(), ora.get_trace())
+    assert abs(cg["leakage"] - cc["leakage"]) <= RTOL * abs(cc["leakage"]) + 1e-300
+
+
+@pytest.mark.parametrize("name,precision,tracking", [("PUa-1-0-IN", "fp64", None), ("PUa-1-0-IN", "mixed", None),
+                                                     ("PUb-1-0-SL", "mixed", None),
+                                                     ("PUa-1-0-SL", "fp64", "implicit-leakage-delta-tracking"),
+                                                     ("PUb-1-0-SL", "mixed", "implicit-leakage-delta-tracking")])
+def test_reference_known_answers_on_gpu(name, precision, tracking):
     deck = DECKS[name]
-    eng = Engine(decks.from_reference_deck(deck, nparticles=100000).build(precision=precision), 0)
+    eng = Engine(decks.from_reference_deck(deck, nparticles=100000, tracking=tracking).build(precision=precision), 0)
     st, _, _ = eng.run_power_iteration(40, 10)
     assert abs(st["kcol_avg"] - deck["_expected_k"]) < 4 * st["kcol_std"] + 2e-4, st
 
