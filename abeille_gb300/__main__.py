@@ -63,7 +63,8 @@ def main(argv=None):
     r.add_argument("--particles", type=int)
     r.add_argument("--generations", type=int)
     r.add_argument("--ignored", type=int)
-    r.add_argument("--tracking", choices=["delta-tracking", "surface-tracking", "implicit-leakage-delta-tracking"])
+    r.add_argument("--tracking", choices=["delta-tracking", "surface-tracking", "implicit-leakage-delta-tracking",
+                                             "carter-tracking"])
     r.add_argument("--device", type=int, default=0)
     w = sub.add_parser("write-config", help="write a synthetic problem as a deck")
     w.add_argument("config", type=int, choices=sorted(decks.CONFIGS))

@@ -27,7 +27,8 @@ QUANTITY = {"flux": 0, "elastic": 1, "absorption": 2, "fission": 3, "total": 4}
 SPATIAL = {"point": 0, "box": 1}
 DIRECTION = {"isotropic": 0, "mono-directional": 1}
 MODE = {"k-eigenvalue": 0, "fixed-source": 1}
-TRACKING = {"delta-tracking": 0, "surface-tracking": 1, "implicit-leakage-delta-tracking": 2}
+TRACKING = {"delta-tracking": 0, "surface-tracking": 1, "implicit-leakage-delta-tracking": 2,
+            "carter-tracking": 3}
 PRECISION = {"fp64": 0, "mixed": 1}
 
 
@@ -79,7 +80,7 @@ class Settings(C.Structure):
     _fields_ = [("mode", C.c_int32), ("tracking", C.c_int32), ("precision", C.c_int32), ("ngroups", C.c_int32),
                 ("seed", C.c_uint64), ("stride", C.c_uint64), ("wgt_cutoff", C.c_double),
                 ("wgt_survival", C.c_double), ("nparticles", C.c_double), ("block_size", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("reserved", C.c_int32), ("wgt_split", C.c_double)]
 
 
 class Problem(C.Structure):
@@ -99,6 +100,7 @@ class Problem(C.Structure):
         ("tally_ebounds", C.POINTER(C.c_double)), ("n_tally_ebounds", C.c_int32),
         ("entropy", EntropyMesh),
         ("sources", C.POINTER(Source)), ("n_sources", C.c_int32),
+        ("sampling_xs_ratio", C.POINTER(C.c_double)),
     ]
 
 

@@ -7,7 +7,7 @@ shared library exposing the C-ABI of include/abeille_gb300.h:
   transport_fp64.cu           FP64 parity transport kernels        --fmad=false
   transport_mixed.cu          FP32-tracking kernels, delta tracking
   transport_mixed_surface.cu  FP32-tracking kernels, surface tracking
-  transport_mixed_ildt.cu     FP32-tracking kernels, implicit-leakage delta tracking
+  transport_mixed_variants.cu FP32-tracking kernels, implicit-leakage and Carter tracking
   server.cpp                  request loop (host scheduler thread)
 
 Host code is compiled with -ffp-contract=off so derived tables round the same
@@ -33,7 +33,7 @@ UNITS = [
     ("transport_fp64.cu", ["--fmad=false"]),
     ("transport_mixed.cu", []),
     ("transport_mixed_surface.cu", []),
-    ("transport_mixed_ildt.cu", []),
+    ("transport_mixed_variants.cu", []),
     ("server.cpp", []),
 ]
 

@@ -150,7 +150,7 @@ static int append_problem(Pools& P, const abx_problem* pr) {
   if (G < 1 || G > 1024) return fail(ABX_ERR_INVALID, "ngroups %d out of range", G);
   if (s.mode != ABX_MODE_K_EIGENVALUE && s.mode != ABX_MODE_FIXED_SOURCE)
     return fail(ABX_ERR_UNSUPPORTED, "simulation mode %d is outside the multigroup transport path", s.mode);
-  if (s.tracking != ABX_TRACK_DELTA && s.tracking != ABX_TRACK_SURFACE && s.tracking != ABX_TRACK_IMPLICIT_LEAKAGE)
+  if (s.tracking < ABX_TRACK_DELTA || s.tracking > ABX_TRACK_CARTER)
     return fail(ABX_ERR_UNSUPPORTED, "tracking mode %d not supported", s.tracking);
   if (!pr->energy_bounds) return fail(ABX_ERR_INVALID, "no energy bounds");
   for (int g = 0; g < G; g++)
@@ -396,8 +396,14 @@ static int append_problem(Pools& P, const abx_problem* pr) {
     }
     P.mats.push_back(M);
   }
-  // majorant (src/majorant.cpp:132-176)
+  // majorant (src/majorant.cpp:132-176), then the sampling cross section of
+  // Carter tracking, majorant x sampling-xs-ratio (src/carter_tracker.cpp:60-72)
   for (int g = 0; g < G; g++) P.maj_d.push_back(maj[g]);
+  for (int g = 0; g < G; g++) {
+    const double ratio = pr->sampling_xs_ratio ? pr->sampling_xs_ratio[g] : 1.0;
+    if (!(ratio > 0.)) return fail(ABX_ERR_INVALID, "sampling-xs-ratio must be positive (group %d)", g);
+    P.maj_d.push_back(maj[g] * ratio);
+  }
   // tallies (src/mesh_tally.cpp:62-119)
   pt.tally_first = (int)P.tallies.size();
   pt.tally_count = pr->n_tallies;
@@ -463,6 +469,10 @@ static int append_problem(Pools& P, const abx_problem* pr) {
   pt.wgt_survival = s.wgt_survival;
   pt.wgt_cutoff_f = (float)s.wgt_cutoff;
   pt.wgt_survival_f = (float)s.wgt_survival;
+  pt.wgt_split = s.wgt_split > 0. ? s.wgt_split : 2.0;  // src/settings.cpp:64
+  pt.wgt_split_f = (float)pt.wgt_split;
+  if (s.tracking == ABX_TRACK_CARTER && !(pt.wgt_split > s.wgt_survival))
+    return fail(ABX_ERR_INVALID, "wgt-split must exceed wgt-survival (src/parser.cpp:689-697)");
   pt.nparticles = s.nparticles;
   pt.inv_np = 1. / s.nparticles;
   pt.min_energy = std::max(0., pr->energy_bounds[0]);  // src/parser.cpp:157-168
@@ -1160,7 +1170,15 @@ static int ensure_sites(abx_ctx* c, size_t n, bool mixed) {
 }
 
 static int ensure_sec(abx_ctx* c, bool mixed) {
-  if (c->prob0.mode != ABX_MODE_FIXED_SOURCE || !c->fissile_any) return ABX_OK;
+  // secondaries: fission in fixed-source problems, splitting in Carter tracking
+  const bool carter = c->prob0.tracking == ABX_TRACK_CARTER;
+  if (!carter && (c->prob0.mode != ABX_MODE_FIXED_SOURCE || !c->fissile_any)) return ABX_OK;
+  if (carter && c->sec_cap < 64) {
+    if (c->sec) cudaFree(c->sec);
+    c->sec = nullptr;
+    c->sec_threads = 0;
+    c->sec_cap = 64;
+  }
   size_t threads = (size_t)c->grid * c->block;
   size_t need = threads * c->sec_cap * 9 * (mixed ? sizeof(float) : sizeof(double));
   if (c->sec && c->sec_threads >= threads) return ABX_OK;
@@ -1596,6 +1614,8 @@ extern "C" int abx_transport_noalloc(abx_ctx* c, const abx_particle* bank_dev, s
                 NA_SITES, site_capacity);
   if (c->prob0.mode == ABX_MODE_FIXED_SOURCE && c->fissile_any)
     return fail(ABX_ERR_UNSUPPORTED, "fixed-source fission secondaries need abx_transport");
+  if (c->prob0.tracking == ABX_TRACK_CARTER)
+    return fail(ABX_ERR_UNSUPPORTED, "Carter tracking splits particles onto stacks: use abx_transport");
   if (cudaSetDevice(c->device) != cudaSuccess) return fail(ABX_ERR_CUDA, "cudaSetDevice failed");
   unsigned char* scratch = nullptr;
   int rc = scratch_address(c->device, &scratch);

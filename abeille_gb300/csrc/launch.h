@@ -43,8 +43,9 @@ int transport_regs_d(int tracking);
 void launch_transport_f(const TransportArgs<float>& A, int tracking, bool iso, bool trace, int grid, int block,
                         cudaStream_t s);
 void launch_transport_f_surface(const TransportArgs<float>& A, bool iso, int grid, int block, cudaStream_t s);
-void launch_transport_f_ildt(const TransportArgs<float>& A, bool iso, int grid, int block, cudaStream_t s);
-int occupancy_f_ildt(bool iso, int block);
+void launch_transport_f_variant(const TransportArgs<float>& A, int tracking, bool iso, int grid, int block,
+                                cudaStream_t s);
+int occupancy_f_variant(int tracking, bool iso, int block);
 int transport_regs_f(int tracking);
 int transport_regs_f_surface();
 

@@ -280,8 +280,7 @@ extern "C" int abx_server_create(const abx_server_options* options, abx_server**
   if (options->nbatches < 1) return srv_fail(ABX_ERR_INVALID, "nbatches must be >= 1");
   if (options->precision != ABX_PREC_FP64 && options->precision != ABX_PREC_MIXED)
     return srv_fail(ABX_ERR_INVALID, "precision %d", options->precision);
-  if (options->tracking != ABX_TRACK_DELTA && options->tracking != ABX_TRACK_SURFACE &&
-      options->tracking != ABX_TRACK_IMPLICIT_LEAKAGE)
+  if (options->tracking < ABX_TRACK_DELTA || options->tracking > ABX_TRACK_CARTER)
     return srv_fail(ABX_ERR_INVALID, "tracking %d", options->tracking);
   abx_server* s = new abx_server();
   s->opt = *options;

@@ -73,7 +73,7 @@ struct ProbT {
   int32_t root;
   int32_t G;
   int32_t eb_off;      // energy bounds (G+1) in the bounds pool
-  int32_t maj_off;     // majorant (G) in the majorant pool
+  int32_t maj_off;     // majorant (G), then the Carter sampling xs (G), in the majorant pool
   int32_t tally_first, tally_count;
   int32_t mode, tracking;
   int32_t has_tle, has_coll;
@@ -88,7 +88,8 @@ struct ProbT {
   double ent_low[3], ent_d[3];
   int32_t src_first, src_count;   // into the source pool
   int32_t src_cdf_off;            // discrete CDF over source weights
-  int32_t pad_;
+  float wgt_split_f;
+  double wgt_split;               // Carter tracking splits at |weight| >= this
 };
 
 struct Tables {

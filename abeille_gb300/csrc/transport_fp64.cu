@@ -10,6 +10,7 @@ template __global__ void transport_kernel<double, ABX_TRACK_DELTA, false>(const 
 template __global__ void transport_kernel<double, ABX_TRACK_SURFACE, false>(const __grid_constant__ TransportArgs<double>);
 template __global__ void transport_kernel<double, ABX_TRACK_IMPLICIT_LEAKAGE, false>(
     const __grid_constant__ TransportArgs<double>);
+template __global__ void transport_kernel<double, ABX_TRACK_CARTER, false>(const __grid_constant__ TransportArgs<double>);
 
 void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace, int grid, int block,
                         cudaStream_t s) {
@@ -17,6 +18,8 @@ void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace
     transport_kernel<double, ABX_TRACK_DELTA, false><<<grid, block, 0, s>>>(A);
   } else if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE) {
     transport_kernel<double, ABX_TRACK_IMPLICIT_LEAKAGE, false><<<grid, block, 0, s>>>(A);
+  } else if (tracking == ABX_TRACK_CARTER) {
+    transport_kernel<double, ABX_TRACK_CARTER, false><<<grid, block, 0, s>>>(A);
   } else {
     transport_kernel<double, ABX_TRACK_SURFACE, false><<<grid, block, 0, s>>>(A);
   }
@@ -29,6 +32,8 @@ int occupancy_d(int tracking, int block) {
   else if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_IMPLICIT_LEAKAGE, false>,
                                                   block, 0);
+  else if (tracking == ABX_TRACK_CARTER)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_CARTER, false>, block, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_SURFACE, false>, block, 0);
   return nb;

@@ -97,6 +97,33 @@ __device__ __noinline__ Bound<R> trk_bc_ool(const Tables& T, const ProbT& P, con
   return sizeof(R) == 8 ? trk_bc(T, V, P, k) : trk_bc_mixed(T, V, P, k);
 }
 
+// Particle::split (include/simulation/particle.hpp:165-173) as Carter tracking
+// applies it after every collision, real or virtual (src/carter_tracker.cpp:
+// 218-222): a weight of magnitude wgt_split or more becomes ceil(|w|)
+// particles of equal weight, the copies on the history's secondary stack.
+template <class R>
+ABX_DEV void carter_split(const TransportArgs<R>& A, const ProbT& P, Lane<R>& L) {
+  if (!(m_abs(L.w) >= (R)P.wgt_split)) return;
+  const int n_new = (int)ceil((double)m_abs(L.w));
+  if (n_new <= 1) return;
+  L.w = L.w / (R)n_new;
+  L.w2 = L.w2 / (R)n_new;
+  const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int i = 0; i < n_new - 1; i++) {
+    if (L.nsec < A.sec_cap) {
+      R* sp = A.sec + ((uint64_t)gt * A.sec_cap + L.nsec) * 9;
+      sp[0] = L.r.x; sp[1] = L.r.y; sp[2] = L.r.z;
+      sp[3] = L.u.x; sp[4] = L.u.y; sp[5] = L.u.z;
+      sp[6] = L.E; sp[7] = L.w; sp[8] = L.w2;
+      L.nsec++;
+    } else {
+      raise_err(A.st, ABX_ERR_CAPACITY, L.h);
+      atomicAdd(&A.st->sec_overflow, 1ull);
+      return;
+    }
+  }
+}
+
 // End of a history: its fission-site count (for the bank sort) and its score
 // totals, to the block's accumulators or, in a batch of problems, to its
 // problem's sums and counters.
@@ -255,9 +282,11 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
             ph = PH_MOVED;
           }
         }
-      } else if (TRACK == ABX_TRACK_DELTA) {
-        // DeltaTracker::transport (src/delta_tracker.cpp:105-118)
-        const R Emaj = V.maj[P.maj_off + L.g];
+      } else if (TRACK == ABX_TRACK_DELTA || TRACK == ABX_TRACK_CARTER) {
+        // DeltaTracker::transport (src/delta_tracker.cpp:105-118); Carter
+        // tracking flies the same way on its sampling cross section
+        // (src/carter_tracker.cpp:124-138), stored after the majorant
+        const R Emaj = V.maj[P.maj_off + (TRACK == ABX_TRACK_CARTER ? P.G : 0) + L.g];
         dcol = Emaj == R(0) ? Tol<R>::INF : -m_log(R(1) - canon<R>(L.rng)) / Emaj;
         trk_move(k, dcol);
         const int r = trk_check(T, V, k, dui, dfr);
@@ -384,7 +413,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
 
     // ----------------------------------------------------------------- moved
     if (ph == PH_MOVED) {
-      if (k.cell < 0 && TRACK == ABX_TRACK_DELTA) {
+      if (k.cell < 0 && (TRACK == ABX_TRACK_DELTA || TRACK == ABX_TRACK_CARTER)) {
         // flew out of the geometry: back to the last position, find the
         // boundary condition (src/delta_tracker.cpp:120-127)
         trk_set_r(k, L.r);
@@ -399,16 +428,39 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
         }
       } else {
         const ProbT& P = T.probs[L.pid];
-        if (TRACK == ABX_TRACK_DELTA && converged && P.has_tle) score_flight(T, V, P, L, dcol);
+        if (TRACK != ABX_TRACK_IMPLICIT_LEAKAGE && converged && P.has_tle) score_flight(T, V, P, L, dcol);
         L.r = add(L.r, scl(L.u, dcol));
         L.mat = T.cells[k.cell].fill;
         const MatT& M = T.mats[L.mat];
         const R Et = V.xs[M.xs_off + XS_ET * M.G + L.g];
-        const R Emaj = V.maj[P.maj_off + L.g];
-        if (Et - Emaj > Tol<R>::MAJ) ABX_FAIL(ABX_ERR_MAJORANT) else {
-          const bool real = canon<R>(L.rng) < (Et / Emaj);
+        if (TRACK == ABX_TRACK_CARTER) {
+          // src/carter_tracker.cpp:184-207: where the sampling cross section
+          // falls below the total one the collision is always "real" with
+          // probability D and carries weight factors +-F
+          const R Es = V.maj[P.maj_off + P.G + L.g];
+          bool real;
+          if (Es >= Et) {
+            real = canon<R>(L.rng) < (Et / Es);
+          } else {
+            const R D = Et / (R(2) * Et - Es);
+            const R F = Et / (D * Es);
+            real = (D - canon<R>(L.rng)) > R(0);
+            L.w = real ? L.w * F : -L.w * F;
+          }
           if (TRACE) trace_rec(A, L, real ? 1 : 0, k.cell);
-          ph = real ? PH_COLL : PH_FLIGHT;
+          if (real) {
+            ph = PH_COLL;
+          } else {
+            carter_split(A, P, L);
+            ph = PH_FLIGHT;
+          }
+        } else {
+          const R Emaj = V.maj[P.maj_off + L.g];
+          if (Et - Emaj > Tol<R>::MAJ) ABX_FAIL(ABX_ERR_MAJORANT) else {
+            const bool real = canon<R>(L.rng) < (Et / Emaj);
+            if (TRACE) trace_rec(A, L, real ? 1 : 0, k.cell);
+            ph = real ? PH_COLL : PH_FLIGHT;
+          }
         }
       }
     }
@@ -451,6 +503,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
       }
       k.u = L.u;
       if (TRACE) trace_rec(A, L, 4, k.cell);
+      if (TRACK == ABX_TRACK_CARTER && alive) carter_split(A, P, L);
       ph = alive ? PH_FLIGHT : PH_DEAD;
     }
 

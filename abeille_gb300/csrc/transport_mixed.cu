@@ -15,8 +15,8 @@ void launch_transport_f(const TransportArgs<float>& A, int tracking, bool iso, b
                         cudaStream_t s) {
   if (tracking == ABX_TRACK_SURFACE) {
     launch_transport_f_surface(A, iso, grid, block, s);
-  } else if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE) {
-    launch_transport_f_ildt(A, iso, grid, block, s);
+  } else if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE || tracking == ABX_TRACK_CARTER) {
+    launch_transport_f_variant(A, tracking, iso, grid, block, s);
   } else if (iso) {
     transport_kernel<float, ABX_TRACK_DELTA, true><<<grid, block, 0, s>>>(A);
   } else {
@@ -26,7 +26,8 @@ void launch_transport_f(const TransportArgs<float>& A, int tracking, bool iso, b
 
 int occupancy_f(int tracking, bool iso, int block) {
   if (tracking == ABX_TRACK_SURFACE) return occupancy_f_surface(iso, block);
-  if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE) return occupancy_f_ildt(iso, block);
+  if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE || tracking == ABX_TRACK_CARTER)
+    return occupancy_f_variant(tracking, iso, block);
   int nb = 0;
   if (iso) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<float, ABX_TRACK_DELTA, true>, block, 0);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<float, ABX_TRACK_DELTA, false>, block, 0);

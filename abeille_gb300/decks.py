@@ -277,7 +277,9 @@ def from_reference_deck(deck, nparticles=None, precision="fp64", tracking=None):
                        mode={"k-eigenvalue": "k-eigenvalue", "fixed-source": "fixed-source"}[st["simulation"]],
                        tracking=tracking or st.get("transport", "surface-tracking"), precision=precision,
                        nparticles=nparticles or int(st["nparticles"]),
-                       seed=int(st.get("seed", 19073486328125)), stride=int(st.get("stride", 152917)))
+                       seed=int(st.get("seed", 19073486328125)), stride=int(st.get("stride", 152917)),
+                       wgt_cutoff=float(st.get("wgt-cutoff", 0.25)), wgt_survival=float(st.get("wgt-survival", 1.0)),
+                       wgt_split=float(st.get("wgt-split", 2.0)), sampling_xs_ratio=deck.get("sampling-xs-ratio"))
     for m in deck["materials"]:
         leg = {l: m[f"P{l}"] for l in range(1, 6) if f"P{l}" in m}
         b.material(int(m["id"]), total=m["total"], absorption=m["absorption"], scatter=m["scatter"],

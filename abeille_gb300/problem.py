@@ -98,7 +98,7 @@ def _ptr(arr, ctype):
 class ProblemBuilder:
     def __init__(self, ngroups, energy_bounds, mode="k-eigenvalue", tracking="delta-tracking",
                  precision="fp64", nparticles=10000, seed=19073486328125, stride=152917,
-                 wgt_cutoff=0.25, wgt_survival=1.0, block_size=0):
+                 wgt_cutoff=0.25, wgt_survival=1.0, block_size=0, wgt_split=2.0, sampling_xs_ratio=None):
         self.G = int(ngroups)
         self.energy_bounds = np.asarray(energy_bounds, dtype=np.float64)
         if self.energy_bounds.shape != (self.G + 1,):
@@ -106,6 +106,8 @@ class ProblemBuilder:
         self.mode, self.tracking, self.precision = mode, tracking, precision
         self.nparticles, self.seed, self.stride = nparticles, seed, stride
         self.wgt_cutoff, self.wgt_survival, self.block_size = wgt_cutoff, wgt_survival, block_size
+        self.wgt_split = wgt_split
+        self.sampling_xs_ratio = None if sampling_xs_ratio is None else [float(x) for x in sampling_xs_ratio]
         self.surfaces, self.cells, self.universes, self.materials = [], [], {}, []
         self.universe_decl = []
         self.tallies, self.sources = [], []
@@ -426,6 +428,7 @@ class ProblemBuilder:
         s.wgt_survival = self.wgt_survival
         s.nparticles = float(self.nparticles)
         s.block_size = self.block_size
+        s.wgt_split = self.wgt_split
         p.energy_bounds = _ptr(eb, C.c_double)
         p.surfaces = C.cast(surf, C.POINTER(abi.Surface))
         p.n_surfaces = len(self.surfaces)
@@ -458,7 +461,13 @@ class ProblemBuilder:
                 p.entropy.hi[a] = self.entropy["hi"][a]
         p.sources = C.cast(src, C.POINTER(abi.Source))
         p.n_sources = len(self.sources)
-        keep = [surf, cells, unis, mats, tal, src, eb, rpn_a, cl_a, le_a, mg_a, teb_a]
+        smp = None
+        if self.sampling_xs_ratio is not None:
+            smp = np.asarray(self.sampling_xs_ratio, dtype=np.float64)
+            if smp.shape != (G,):
+                raise ValueError("sampling_xs_ratio needs one entry per group")
+            p.sampling_xs_ratio = _ptr(smp, C.c_double)
+        keep = [surf, cells, unis, mats, tal, src, eb, rpn_a, cl_a, le_a, mg_a, teb_a, smp]
         meta = {"universe_order": order, "tally_shapes": [t["shape"] for t in self.tallies],
                 "tally_ne": [len(t["eb"]) - 1 for t in self.tallies], "ngroups": G,
                 "nparticles": self.nparticles, "mode": self.mode}

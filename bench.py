@@ -189,7 +189,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tracking", default=None,
-                    choices=["delta-tracking", "surface-tracking", "implicit-leakage-delta-tracking"])
+                    choices=["delta-tracking", "surface-tracking", "implicit-leakage-delta-tracking", "carter-tracking"])
     ap.add_argument("--problems", type=int, default=4096, help="config 3: problems in the batch")
     ap.add_argument("--per-problem-sample", type=int, default=128,
                     help="config 3/4: problems timed one launch per problem")

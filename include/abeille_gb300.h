@@ -180,8 +180,9 @@ typedef struct abx_source {
 enum { ABX_MODE_K_EIGENVALUE = 0, ABX_MODE_FIXED_SOURCE = 1 };
 /* Transporters: DeltaTracker (src/delta_tracker.cpp), SurfaceTracker
  * (src/surface_tracker.cpp), ImplicitLeakageDeltaTracker
- * (src/implicit_leakage_delta_tracker.cpp). */
-enum { ABX_TRACK_DELTA = 0, ABX_TRACK_SURFACE = 1, ABX_TRACK_IMPLICIT_LEAKAGE = 2 };
+ * (src/implicit_leakage_delta_tracker.cpp), CarterTracker
+ * (src/carter_tracker.cpp). */
+enum { ABX_TRACK_DELTA = 0, ABX_TRACK_SURFACE = 1, ABX_TRACK_IMPLICIT_LEAKAGE = 2, ABX_TRACK_CARTER = 3 };
 /* ABX_PREC_FP64: every operation in double, reference draw order, no FMA
  *   contraction: reproduces the reference per history.
  * ABX_PREC_MIXED: positions, directions, flight distances and cross sections
@@ -201,6 +202,8 @@ typedef struct abx_settings {
   double nparticles;  /* tally net weight == particles per generation (src/tallies.cpp:79) */
   int32_t block_size; /* 0 = autotuned                                      */
   int32_t reserved;
+  double wgt_split;   /* 2.0 (src/settings.cpp:64): Carter tracking splits a
+                         particle whose |weight| reaches it                  */
 } abx_settings;
 
 /* ------------------------------------------------------------- problem */
@@ -220,6 +223,9 @@ typedef struct abx_problem {
   const double* tally_ebounds;   int32_t n_tally_ebounds;
   abx_entropy_mesh entropy;
   const abx_source* sources;     int32_t n_sources;
+  /* Carter tracking: per-group ratio of the sampling cross section to the
+   * majorant (deck "sampling-xs-ratio", src/parser.cpp:425-434); NULL = 1. */
+  const double* sampling_xs_ratio;
 } abx_problem;
 
 /* ------------------------------------------------------- particle banks */

@@ -227,6 +227,7 @@ struct oracle_ctx {
   int* n_dg; double** dg_cdf; double** dg_lambda;
   AngleTab* ang; double* ang_mu; double* ang_pdf; double* ang_cdf; int ang_n;
   double* maj;
+  double* smp;   /* Carter tracking sampling cross section per group */
   /* tallies */
   int ntally; OTally* tally;
   int ent_on; int ent_shape[3]; double ent_low[3], ent_d[3];
@@ -1141,6 +1142,8 @@ static int run_history(oracle_ctx* ctx, const abx_particle* in, uint32_t h, doub
   int mat = t.cell >= 0 ? ctx->cell[t.cell].fill : -1;
   const int delta = ctx->set.tracking == ABX_TRACK_DELTA;
   const int ildt = ctx->set.tracking == ABX_TRACK_IMPLICIT_LEAKAGE;
+  const int carter = ctx->set.tracking == ABX_TRACK_CARTER;
+  const double wgt_split = ctx->set.wgt_split > 0. ? ctx->set.wgt_split : 2.0;
   int rc = ABX_OK;
   while (p.alive) {
     int had_collision = 0;
@@ -1214,8 +1217,10 @@ static int run_history(oracle_ctx* ctx, const abx_particle* in, uint32_t h, doub
         if (oracle_canonical(&p.rng) < (Et / Emaj)) had_collision = 1;
         trace(ctx, tb, h, had_collision ? 1 : 0, &p, t.cell);
       }
-    } else if (delta) {
-      double Emaj = ctx->maj[g];
+    } else if (delta || carter) {
+      /* CarterTracker::transport (src/carter_tracker.cpp:124-222) flies like
+       * the delta tracker, on its sampling cross section */
+      double Emaj = carter ? ctx->smp[g] : ctx->maj[g];
       double d_coll = oracle_exponential(&p.rng, Emaj);
       Boundary bound = {INF_, -1, ABX_BC_NORMAL, 0};
       int crossed = 0;
@@ -1255,11 +1260,28 @@ static int run_history(oracle_ctx* ctx, const abx_particle* in, uint32_t h, doub
         p.s.r = vadd(p.s.r, vscale(p.s.u, d_coll));
         mat = ctx->cell[t.cell].fill;
         double Et = MAT_AT(ctx->Et, mat, g);
-        if (Et - Emaj > 1.E-10) {
-          set_err("Total cross section excedeed majorant: Et = %g, Emaj = %g", Et, Emaj);
-          return ABX_ERR_MAJORANT;
+        if (carter) {
+          /* src/carter_tracker.cpp:188-207 */
+          const double Esample = Emaj;
+          if (Esample >= Et) {
+            if (oracle_canonical(&p.rng) < (Et / Esample)) had_collision = 1;
+          } else {
+            double D = Et / (2. * Et - Esample);
+            double F = Et / (D * Esample);
+            if ((D - oracle_canonical(&p.rng)) > 0.) {
+              p.s.w = p.s.w * F;
+              had_collision = 1;
+            } else {
+              p.s.w = -p.s.w * F;
+            }
+          }
+        } else {
+          if (Et - Emaj > 1.E-10) {
+            set_err("Total cross section excedeed majorant: Et = %g, Emaj = %g", Et, Emaj);
+            return ABX_ERR_MAJORANT;
+          }
+          if (oracle_canonical(&p.rng) < (Et / Emaj)) had_collision = 1;
         }
-        if (oracle_canonical(&p.rng) < (Et / Emaj)) had_collision = 1;
         trace(ctx, tb, h, had_collision ? 1 : 0, &p, t.cell);
       }
     } else {
@@ -1314,6 +1336,16 @@ static int run_history(oracle_ctx* ctx, const abx_particle* in, uint32_t h, doub
       if (rc) return rc;
       t.u = p.s.u;
       trace(ctx, tb, h, 4, &p, t.cell);
+    }
+    if (carter && p.alive && fabs(p.s.w) >= wgt_split) {
+      /* Particle::split (include/simulation/particle.hpp:165-173) */
+      int n_new = (int)ceil(fabs(p.s.w));
+      if (n_new > 1) {
+        p.s.w = p.s.w / (double)n_new;
+        p.s.w2 = p.s.w2 / (double)n_new;
+        for (int k = 0; k < n_new - 1; k++)
+          if (!sec_push(&p, p.s)) { set_err("out of memory"); return ABX_ERR_OOM; }
+      }
     }
     if (!p.alive) {
       resurrect(&p);
@@ -1786,7 +1818,7 @@ void oracle_destroy(oracle_ctx* ctx) {
   free(ctx->Es); free(ctx->vEf); free(ctx->ps_cdf); free(ctx->chi_cdf); free(ctx->fissile);
   if (ctx->dg_cdf) for (int m = 0; m < ctx->M; m++) { free(ctx->dg_cdf[m]); free(ctx->dg_lambda[m]); }
   free(ctx->dg_cdf); free(ctx->dg_lambda); free(ctx->n_dg);
-  free(ctx->ang); free(ctx->ang_mu); free(ctx->ang_pdf); free(ctx->ang_cdf); free(ctx->maj);
+  free(ctx->ang); free(ctx->ang_mu); free(ctx->ang_pdf); free(ctx->ang_cdf); free(ctx->maj); free(ctx->smp);
   for (int t = 0; t < ctx->ntally; t++) {
     free(ctx->tally[t].eb); free(ctx->tally[t].gen); free(ctx->tally[t].avg); free(ctx->tally[t].var);
   }
@@ -2005,6 +2037,10 @@ int oracle_create(const abx_problem* P, oracle_ctx** out) {
       double xs = MAT_AT(ctx->Et, m, g);
       if (xs > ctx->maj[g]) ctx->maj[g] = xs;
     }
+  /* CarterTracker ctor (src/carter_tracker.cpp:60-72): the majorant at the
+   * group's mid energy times the deck's sampling-xs-ratio */
+  ctx->smp = (double*)xcalloc((size_t)G, sizeof(double));
+  for (int g = 0; g < G; g++) ctx->smp[g] = ctx->maj[g] * (P->sampling_xs_ratio ? P->sampling_xs_ratio[g] : 1.0);
   /* tallies */
   ctx->ntally = P->n_tallies;
   ctx->tally = (OTally*)xcalloc((size_t)P->n_tallies, sizeof(OTally));

@@ -305,3 +305,32 @@ def test_autotuned_launch_shape_gives_the_same_results():
     assert close(s0["r"], s1["r"], atol=0) and c0["collisions"] == c1["collisions"]
     assert abs(c0["k_col"] - c1["k_col"]) <= RTOL * abs(c0["k_col"])
     eng.close()
+
+
+@pytest.mark.parametrize("case", ["keig-1.3", "fixed-0.9"])
+def test_carter_tracking_matches(case):
+    """CarterTracker against the oracle, FP64: per-event traces, scores and
+    collision counts; `fixed-0.9` samples 10 % below the total cross section
+    (signed weights, splitting onto the secondary stack)."""
+    if case == "keig-1.3":
+        b = decks.config0(nparticles=512, tracking="carter-tracking")
+        b.sampling_xs_ratio = [1.3] * b.G
+    else:
+        b = decks.fixed_source_problem(3, precision="fp64", nparticles=512, tracking="carter-tracking")
+        b.sampling_xs_ratio = [0.9] * b.G
+    eng, ora, _ = pair(b)
+    bank = ora.sample_sources(0, 512)
+    eng.set_trace(128, 1 << 21)
+    ora.set_trace(128, 1 << 21)
+    sg, cg = eng.transport(bank, 1.0, True)
+    sc, cc = ora.transport(bank, 1.0, True)
+    compare_traces(eng.get_trace(), ora.get_trace())
+    assert cg["collisions"] == cc["collisions"] and cg["flights"] == cc["flights"]
+    for k in ("k_col", "leakage", "mig_area"):
+        assert abs(cg[k] - cc[k]) <= 1e-11 * abs(cc[k]) + 1e-300, (k, cg[k], cc[k])
+    if case == "fixed-0.9":
+        st_g = eng.run_fixed_source(3, 512)
+        st_c = ora.run_fixed_source(3, 512)
+        assert st_g["collisions"] == st_c["collisions"]
+        assert abs(st_g["leak_avg"] - st_c["leak_avg"]) <= 1e-11 * abs(st_c["leak_avg"])
+    eng.close()
