@@ -553,9 +553,9 @@ def bench_server(args):
 
 
 # DRAM bytes (read + write) per history of a transport launch, from the ncu
-# capture in profiles/transport_kernel_config1_mixed_300k.md (158.1 MB at
+# capture in profiles/transport_kernel_config1_mixed_300k.md (274.2 MB at
 # 300,000 histories); bank, site and spill traffic grow with the histories.
-TRAFFIC_PER_HISTORY = {(1, "mixed"): 158.12e6 / 3e5}
+TRAFFIC_PER_HISTORY = {(1, "mixed"): 274.21e6 / 3e5}
 L2_FLUSH_BYTES = 256 << 20
 
 if __name__ == "__main__":
