@@ -2103,22 +2103,69 @@ extern "C" int abx_run_fixed_source(abx_ctx* c, int nbatches, uint64_t npart, ab
   return ABX_OK;
 }
 
+// abx_batch_replace in two halves, for callers that derive the next batch's
+// tables on the host while the GPU still runs the current batch: the host
+// half touches no device state; the device half uploads into the context.
+namespace abx {
+struct PreparedBatch {
+  Pools P;
+  int n = 0, tracking = 0, prec = 0;
+};
+
+void* batch_prepare(const abx_problem* problems, int n_problems, int* rc_out) {
+  int rc = ABX_OK;
+  PreparedBatch* b = nullptr;
+  if (!problems || n_problems <= 0) {
+    rc = fail(ABX_ERR_INVALID, "bad arguments");
+  } else {
+    b = new PreparedBatch();
+    b->n = n_problems;
+    b->tracking = problems[0].settings.tracking;
+    b->prec = problems[0].settings.precision;
+    for (int i = 0; i < n_problems && rc == ABX_OK; i++) {
+      const abx_settings& s = problems[i].settings;
+      if (s.mode != ABX_MODE_FIXED_SOURCE || s.tracking != b->tracking || s.precision != b->prec)
+        rc = fail(ABX_ERR_UNSUPPORTED,
+                  "problem %d: a batch holds fixed-source problems of one tracking mode and precision", i);
+      else
+        rc = append_problem(b->P, &problems[i]);
+    }
+    if (rc) {
+      delete b;
+      b = nullptr;
+    }
+  }
+  if (rc_out) *rc_out = rc;
+  return b;
+}
+
+void batch_discard(void* prepared) { delete static_cast<PreparedBatch*>(prepared); }
+
+static int install_prepared(abx_ctx* c, PreparedBatch* b);
+
+int batch_install(abx_ctx* c, void* prepared) {
+  PreparedBatch* b = static_cast<PreparedBatch*>(prepared);
+  int rc = (c && b) ? install_prepared(c, b) : fail(ABX_ERR_INVALID, "bad arguments");
+  delete b;
+  return rc;
+}
+}  // namespace abx
+
 extern "C" int abx_batch_replace(abx_ctx* c, const abx_problem* problems, int n_problems) {
-  if (!c || !problems || n_problems <= 0) return fail(ABX_ERR_INVALID, "bad arguments");
-  for (int i = 0; i < n_problems; i++) {
-    const abx_settings& s = problems[i].settings;
-    if (s.mode != ABX_MODE_FIXED_SOURCE || s.tracking != c->prob0.tracking || s.precision != c->prec)
-      return fail(ABX_ERR_UNSUPPORTED,
-                  "problem %d: a batch holds fixed-source problems of the context's tracking mode and precision", i);
-  }
-  Pools P2;
-  for (int i = 0; i < n_problems; i++) {
-    int rc = append_problem(P2, &problems[i]);
-    if (rc) return rc;  // the context keeps its previous problems
-  }
+  if (!c) return fail(ABX_ERR_INVALID, "bad arguments");
+  int rc;
+  void* b = abx::batch_prepare(problems, n_problems, &rc);
+  if (rc) return rc;  // the context keeps its previous problems
+  return abx::batch_install(c, b);
+}
+
+static int abx::install_prepared(abx_ctx* c, PreparedBatch* b) {
+  if (b->tracking != c->prob0.tracking || b->prec != c->prec)
+    return fail(ABX_ERR_UNSUPPORTED, "the batch's tracking mode or precision differs from the context's");
+  const int n_problems = b->n;
   cudaSetDevice(c->device);
   CUDA_TRY(cudaStreamSynchronize(c->stream));
-  c->P = std::move(P2);
+  c->P = std::move(b->P);
   c->nprob = n_problems;
   c->prob0 = c->P.probs[0];
   c->fissile_any = false;

@@ -1,13 +1,15 @@
 // Request loop for fixed-source problems: a host scheduler over the C-ABI.
 //
 // Submission copies the problem (the caller's buffers are not retained) and
-// queues it with an estimate of its device footprint.  One scheduler thread
-// runs rounds: it admits queued requests in arrival order while the sum of
-// their footprints fits the HBM budget, loads them into its batch context
-// (created on the first round, its device buffers reused afterwards), runs
-// every batch of every admitted request in one transport launch, and copies
-// results and tally bins back.  Requests that arrive during a round wait for the next one, so the
-// rounds size themselves to the arrival rate.
+// queues it with an estimate of its device footprint.  Rounds go through two
+// threads.  The preparation thread admits queued requests in arrival order
+// while the sum of their footprints fits the HBM budget and derives the
+// round's tables on the host; the GPU thread installs a prepared round into
+// its batch context (created on the first round, its device buffers reused
+// afterwards), runs every batch of every admitted request in one transport
+// launch, and copies results and tally bins back.  The next round is prepared
+// while the current one runs on the GPU.  Requests that arrive meanwhile wait
+// for a later round, so the rounds size themselves to the arrival rate.
 //
 // A request's results do not depend on its round: batch b of a problem
 // always transports its histories b*n .. (b+1)*n-1, each seeded by skip-ahead
@@ -30,6 +32,10 @@
 
 namespace abx {
 void set_error_string(const char* msg);  // engine.cu: the thread's abx_last_error_string
+// engine.cu: abx_batch_replace in a host half and a device half
+void* batch_prepare(const abx_problem* problems, int n_problems, int* rc);
+int batch_install(abx_ctx* c, void* prepared);
+void batch_discard(void* prepared);
 }
 
 namespace {
@@ -123,6 +129,14 @@ struct Done {
   std::vector<double> avg, var;
 };
 
+struct Round {
+  std::vector<Request> reqs;
+  void* prepared = nullptr;  // host tables of the batch
+  int number = 0;
+  Clock::time_point t_admit;
+  double prep_ms = 0.;
+};
+
 }  // namespace
 
 struct abx_server {
@@ -135,14 +149,26 @@ struct abx_server {
   uint64_t next_id = 1;
   bool stop = false;
   abx_server_stats stats{};
-  std::thread worker;
+  std::thread worker, preparer;
   int round = 0;
-  abx_ctx* ctx = nullptr;  // owned by the scheduler thread
+  abx_ctx* ctx = nullptr;  // owned by the GPU thread
+  std::unique_ptr<Round> staged;  // prepared, waiting for the GPU thread
+  bool prep_done = false;         // the preparation thread has exited
+  std::condition_variable cv_staged;
 
-  void run_round(std::vector<Request>& reqs, Clock::time_point t_start);
+  void run_round(Round& rd);
   void finish(Request& q, Done&& d, double queue_ms);
+  void fail_request(Request& q, int status, double queue_ms);
+  void prep_loop();
   void loop();
 };
+
+void abx_server::fail_request(Request& q, int status, double queue_ms) {
+  Done d;
+  d.r.status = status;
+  d.r.n_tallies = q.prob->p.n_tallies;
+  finish(q, std::move(d), queue_ms);
+}
 
 void abx_server::finish(Request& q, Done&& d, double queue_ms) {
   d.r.request_id = q.id;
@@ -157,23 +183,23 @@ void abx_server::finish(Request& q, Done&& d, double queue_ms) {
   cv_done.notify_all();
 }
 
-void abx_server::run_round(std::vector<Request>& reqs, Clock::time_point t_start) {
+void abx_server::run_round(Round& rd) {
+  std::vector<Request>& reqs = rd.reqs;
   const int n = (int)reqs.size();
-  std::vector<abx_problem> arr((size_t)n);
-  for (int i = 0; i < n; i++) arr[(size_t)i] = reqs[(size_t)i].prob->p;
+  const Clock::time_point t_start = rd.t_admit;
   const Clock::time_point c0 = Clock::now();
-  // the server's context is kept across rounds; a round swaps its problems in
-  int rc = ctx ? abx_batch_replace(ctx, arr.data(), n) : abx_create_batch(arr.data(), n, opt.device, &ctx);
-  const Clock::time_point c1 = Clock::now();
-  if (rc != ABX_OK && n > 1) {
-    // one of them is malformed: run each alone so the others still complete
-    for (int i = 0; i < n; i++) {
-      std::vector<Request> one;
-      one.push_back(std::move(reqs[(size_t)i]));
-      run_round(one, t_start);
-    }
-    return;
+  // the context is kept across rounds; a round installs its prepared tables
+  int rc;
+  if (ctx) {
+    rc = abx::batch_install(ctx, rd.prepared);
+  } else {
+    abx::batch_discard(rd.prepared);
+    std::vector<abx_problem> arr((size_t)n);
+    for (int i = 0; i < n; i++) arr[(size_t)i] = reqs[(size_t)i].prob->p;
+    rc = abx_create_batch(arr.data(), n, opt.device, &ctx);
   }
+  rd.prepared = nullptr;
+  const Clock::time_point c1 = Clock::now();
   std::vector<abx_problem_result> res((size_t)n);
   abx_run_stats st{};
   if (rc == ABX_OK) rc = abx_run_fixed_source_batch(ctx, opt.nbatches, res.data(), &st);
@@ -198,7 +224,7 @@ void abx_server::run_round(std::vector<Request>& reqs, Clock::time_point t_start
   {
     std::lock_guard<std::mutex> g(mu);
     stats.rounds++;
-    stats.load_ms += ms_between(c0, c1);
+    stats.load_ms += rd.prep_ms + ms_between(c0, c1);
     stats.run_ms += ms_between(c1, c2);
     stats.readback_ms += ms_between(c2, c3);
     stats.free_ms += ms_between(c3, c4);
@@ -210,12 +236,11 @@ void abx_server::run_round(std::vector<Request>& reqs, Clock::time_point t_start
     }
   }
   uint64_t bin0 = 0;
-  const int this_round = round;
   for (int i = 0; i < n; i++) {
     Request& q = reqs[(size_t)i];
     Done d;
     d.r.status = rc;
-    d.r.round = this_round;
+    d.r.round = rd.number;
     d.r.round_problems = n;
     d.r.n_tallies = q.prob->p.n_tallies;
     d.r.n_tally_bins = q.prob->tally_bins();
@@ -231,26 +256,78 @@ void abx_server::run_round(std::vector<Request>& reqs, Clock::time_point t_start
   }
 }
 
-void abx_server::loop() {
+// Preparation thread: admits the next round and derives its host tables while
+// the GPU thread runs the current one.  A request whose problem cannot be
+// prepared fails on its own; the others of its round still run.
+void abx_server::prep_loop() {
+  auto prepare = [](std::vector<Request>& rs, int* rc) {
+    std::vector<abx_problem> arr(rs.size());
+    for (size_t i = 0; i < rs.size(); i++) arr[i] = rs[i].prob->p;
+    return abx::batch_prepare(arr.data(), (int)arr.size(), rc);
+  };
   for (;;) {
-    std::vector<Request> reqs;
+    std::unique_ptr<Round> rd(new Round());
     {
       std::unique_lock<std::mutex> lk(mu);
-      cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+      cv_work.wait(lk, [&] { return stop || (!queue.empty() && !staged); });
       if (stop) break;
       uint64_t used = 0;
       while (!queue.empty()) {
         const Request& h = queue.front();
-        if (!reqs.empty() && used + h.footprint > opt.hbm_budget_bytes) break;
-        if (opt.max_round_problems > 0 && (int)reqs.size() >= opt.max_round_problems) break;
+        if (!rd->reqs.empty() && used + h.footprint > opt.hbm_budget_bytes) break;
+        if (opt.max_round_problems > 0 && (int)rd->reqs.size() >= opt.max_round_problems) break;
         used += h.footprint;
-        reqs.push_back(std::move(queue.front()));
+        rd->reqs.push_back(std::move(queue.front()));
         queue.pop_front();
       }
-      round++;
+      rd->number = ++round;
+    }
+    rd->t_admit = Clock::now();
+    int rc = ABX_OK;
+    rd->prepared = prepare(rd->reqs, &rc);
+    if (rc != ABX_OK) {
+      // isolate the malformed requests
+      std::vector<Request> good;
+      for (Request& q : rd->reqs) {
+        std::vector<Request> one;
+        one.push_back(std::move(q));
+        int rc1 = ABX_OK;
+        abx::batch_discard(prepare(one, &rc1));
+        if (rc1 != ABX_OK) fail_request(one[0], rc1, ms_between(one[0].t_submit, rd->t_admit));
+        else good.push_back(std::move(one[0]));
+      }
+      rd->reqs = std::move(good);
+      rc = ABX_OK;
+      rd->prepared = rd->reqs.empty() ? nullptr : prepare(rd->reqs, &rc);
+      if (rd->reqs.empty()) continue;
+      if (rc != ABX_OK) {
+        for (Request& q : rd->reqs) fail_request(q, rc, ms_between(q.t_submit, rd->t_admit));
+        continue;
+      }
+    }
+    rd->prep_ms = ms_between(rd->t_admit, Clock::now());
+    std::lock_guard<std::mutex> g(mu);
+    staged = std::move(rd);
+    cv_staged.notify_all();
+  }
+  std::lock_guard<std::mutex> g(mu);
+  prep_done = true;
+  cv_staged.notify_all();
+}
+
+// GPU thread: runs the prepared rounds one after the other.
+void abx_server::loop() {
+  for (;;) {
+    std::unique_ptr<Round> rd;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_staged.wait(lk, [&] { return staged || prep_done; });
+      if (!staged) break;
+      rd = std::move(staged);
+      cv_work.notify_all();  // the preparation thread may stage the next round
     }
     const Clock::time_point t0 = Clock::now();
-    run_round(reqs, t0);
+    run_round(*rd);
     std::lock_guard<std::mutex> g(mu);
     stats.busy_ms += ms_between(t0, Clock::now());
   }
@@ -286,6 +363,7 @@ extern "C" int abx_server_create(const abx_server_options* options, abx_server**
   s->opt = *options;
   if (!s->opt.hbm_budget_bytes) s->opt.hbm_budget_bytes = 150ull * 1000 * 1000 * 1000;
   s->worker = std::thread([s] { s->loop(); });
+  s->preparer = std::thread([s] { s->prep_loop(); });
   *out = s;
   return ABX_OK;
 }
@@ -297,7 +375,10 @@ extern "C" int abx_server_destroy(abx_server* s) {
     s->stop = true;
   }
   s->cv_work.notify_all();
+  s->cv_staged.notify_all();
+  if (s->preparer.joinable()) s->preparer.join();
   if (s->worker.joinable()) s->worker.join();
+  if (s->staged && s->staged->prepared) abx::batch_discard(s->staged->prepared);
   delete s;
   return ABX_OK;
 }
