@@ -36,6 +36,16 @@ BYTES = {"fp64": {"flight": 112, "collision": 160, "site": 96},
          "mixed": {"flight": 76, "collision": 108, "site": 96}}
 KERNELS_PER_GEN = 8  # step_begin, transport, 3 x scan, next_bank, tally_record, gen_end
 
+# what each --config is (the synthetic decks of abeille_gb300.decks)
+WORKLOADS = {
+    0: "17x17 pin lattice, 2 materials, 7 groups, k-eigenvalue, 17x17x1 collision flux tally",
+    1: "51x51 pins x 10 axial zones (200 cm), 3 materials, 7 groups, k-eigenvalue, 51x51x20 collision flux tally",
+    2: "17x17 pins with fuel/gap/clad rings, 8 fuels, 70 groups with P1 scattering, k-eigenvalue, "
+       "100x100x50 track-length flux tally",
+    3: "4096 fixed-source slab boxes (1-4 slabs, G in 7/22/44), 10 batches each, 20x20x20 collision flux tallies",
+    4: "request loop: fixed-source slab problems arriving as a Poisson stream",
+}
+
 
 def peaks():
     try:
@@ -136,7 +146,7 @@ def run_reference(args):
         "metric": "collisions/s", "value": value, "unit": "collisions/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"config{args.config}", "histories_per_step": args.ref_sample,
+        "config": {"workload": WORKLOADS[args.config], "deck": args.config, "histories_per_step": args.ref_sample,
                    "tracking": "delta", "precision": "fp64"},
         "cpu_baseline": {"value": value, "unit": "collisions/s", "cores": cores, "kind": "port",
                          "sample": f"{args.ref_sample} first-generation histories of config {args.config} per step"},
@@ -278,7 +288,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": step_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32-track/f64-tally" if args.precision == "mixed" else "f64",
         "data": "synthetic",
-        "config": {"workload": f"config{args.config}", "histories_per_generation": npart,
+        "config": {"workload": WORKLOADS[args.config], "deck": args.config, "histories_per_generation": npart,
                    "tracking": builder.tracking, "precision": args.precision,
                    "l2": f"flushed: {L2_FLUSH_BYTES >> 20} MiB written before each generation, outside its "
                    "timed events", "parallelism": f"replicas{world}",
@@ -392,7 +402,7 @@ def bench_batch(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-track/f64-tally" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": "config3", "problems": args.problems, "histories_per_step": hist_per_step,
+        "config": {"workload": WORKLOADS[3], "deck": 3, "problems": args.problems, "histories_per_step": hist_per_step,
                    "batches": nb, "tracking": builders[0].tracking, "precision": args.precision,
                    "l2": "inputs larger than L2 (bank of all problems' batch, tallies of 4096x8000 bins)",
                    "parallelism": f"replicas{world}"},
@@ -534,7 +544,7 @@ def bench_server(args):
         "steps": len(rates), "warmup": 1, "ms_per_step": 1e3 * args.duration, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-track/f64-tally" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": "config4", "arrivals": "poisson", "rates": rates, "duration_s": args.duration,
+        "config": {"workload": WORKLOADS[4], "deck": 4, "arrivals": "poisson", "rates": rates, "duration_s": args.duration,
                    "problem_pool": npool, "batches": nb, "hbm_budget_gb": args.budget_gb,
                    "precision": args.precision, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 at the high rates (rounds of thousands of problems)"},
