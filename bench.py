@@ -115,6 +115,20 @@ def dist_setup(n):
     return rank, world, local, dist
 
 
+def combine_replicas(dist, seconds, collisions, device):
+    """Whole-job figures of N independent replicas: the slowest rank's device
+    time and the collisions of all ranks (no data-path collective: only these
+    two numbers cross ranks)."""
+    if not dist:
+        return seconds, float(collisions)
+    import torch
+    t = torch.tensor([seconds, float(collisions)], dtype=torch.float64, device=device)
+    tmax = t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(tmax[0]), float(t[1])
+
+
 def cpu_baseline(config, nhist, precision_label="fp64"):
     """The oracle (CPU restatement of the reference, FP64) on all host cores, one
     bounded transport sample of the same workload."""
@@ -247,15 +261,7 @@ def main():
     coll = sum(r["collisions"] for r in recs)
     flights = sum(r["flights"] for r in recs)
     sites = sum(r["sites"] for r in recs)
-    if dist:
-        import torch
-        t = torch.tensor([step_ms / 1e3, float(coll)], dtype=torch.float64, device=f"cuda:{local}")
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        secs, coll_all = float(tmax[0]), float(t[1])
-    else:
-        secs, coll_all = step_ms / 1e3, float(coll)
+    secs, coll_all = combine_replicas(dist, step_ms / 1e3, coll, f"cuda:{local}")
     value = coll_all / secs
 
     e2e = None
@@ -357,15 +363,7 @@ def bench_batch(args):
             flights += st["flights"]
             step_ms += st["total_ms"]
             tr_ms += st["transport_ms"]
-    if dist:
-        import torch
-        t = torch.tensor([step_ms / 1e3, float(coll)], dtype=torch.float64, device=f"cuda:{local}")
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        secs, coll_all = float(tmax[0]), float(t[1])
-    else:
-        secs, coll_all = step_ms / 1e3, float(coll)
+    secs, coll_all = combine_replicas(dist, step_ms / 1e3, coll, f"cuda:{local}")
     eng.close()
     if rank != 0:
         if dist:
