@@ -1100,17 +1100,6 @@ template <class R> __global__ void k_bank_to_aos(BankT<R> b, size_t n, abx_parti
     out[i] = p;
   }
 }
-// double bank -> float bank (mixed mode source sampling)
-__global__ void k_bank_d2f(BankT<double> a, BankT<float> b, size_t off, size_t n) {
-  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
-    size_t i = off + j;
-    b.x[i] = (float)a.x[i]; b.y[i] = (float)a.y[i]; b.z[i] = (float)a.z[i];
-    b.ux[i] = (float)a.ux[i]; b.uy[i] = (float)a.uy[i]; b.uz[i] = (float)a.uz[i];
-    b.E[i] = (float)a.E[i]; b.w[i] = (float)a.w[i]; b.w2[i] = (float)a.w2[i];
-    b.rng[i] = a.rng[i]; b.hid[i] = a.hid[i]; b.fam[i] = a.fam[i];
-    if (a.prob && b.prob) b.prob[i] = a.prob[i];
-  }
-}
 // Sorted sites -> AoS BankedParticles.
 template <class R>
 __global__ void k_sites_to_aos(SiteT<R> S, const DevState* st, const uint32_t* off, BankT<R> cur, abx_site* out,
@@ -1150,8 +1139,9 @@ static int ensure_counts(abx_ctx* c, size_t n) {
 
 static int ensure_banks(abx_ctx* c, size_t n, bool mixed, bool with_prob) {
   int rc;
+  // banks of the transport precision only (mixed runs sample in FP32)
   for (int i = 0; i < 2; i++) {
-    if (c->bd[i].cap < n || (with_prob && !c->bd[i].b.prob))
+    if (!mixed && (c->bd[i].cap < n || (with_prob && !c->bd[i].b.prob)))
       if ((rc = c->bd[i].alloc(n, with_prob)) != ABX_OK) return rc;
     if (mixed && (c->bf[i].cap < n || (with_prob && !c->bf[i].b.prob)))
       if ((rc = c->bf[i].alloc(n, with_prob)) != ABX_OK) return rc;
@@ -1352,6 +1342,25 @@ extern "C" int abx_destroy(abx_ctx* c) {
 
 static bool mixed_of(const abx_ctx* c) { return c->prec == ABX_PREC_MIXED; }
 
+// Samples S.n source histories into bank 0 of the transport precision: FP64
+// runs sample in FP64 (the reference's arithmetic), mixed runs sample in FP32
+// straight into the float bank.  S carries the tables, counts and segments.
+static void sample_bank0(abx_ctx* c, SourceArgs& S, bool mixed, bool with_prob) {
+  S.out_off = 0;
+  S.st = c->st;
+  if (mixed) {
+    BankT<float>& b = c->bf[0].b;
+    S.fx = b.x; S.fy = b.y; S.fz = b.z; S.fux = b.ux; S.fuy = b.uy; S.fuz = b.uz; S.fE = b.E; S.fw = b.w;
+    S.fw2 = b.w2; S.rng = b.rng; S.hid = b.hid; S.fam = b.fam; S.probv = with_prob ? b.prob : nullptr;
+    launch_sources_f(S, c->stream);
+  } else {
+    BankT<double>& b = c->bd[0].b;
+    S.x = b.x; S.y = b.y; S.z = b.z; S.ux = b.ux; S.uy = b.uy; S.uz = b.uz; S.E = b.E; S.w = b.w;
+    S.w2 = b.w2; S.rng = b.rng; S.hid = b.hid; S.fam = b.fam; S.probv = with_prob ? b.prob : nullptr;
+    launch_sources(S, c->stream);
+  }
+}
+
 extern "C" int abx_sample_sources(abx_ctx* c, uint64_t first, size_t n, abx_particle* out) {
   if (!c || (!out && n)) return fail(ABX_ERR_INVALID, "bad arguments");
   if (c->prob0.src_count <= 0) return fail(ABX_ERR_INVALID, "problem has no sources");
@@ -1470,11 +1479,7 @@ extern "C" int abx_autotune(abx_ctx* c, size_t n_probe, int* block_out, int* gri
   S.prob = 0;
   S.first_hid = 0;
   S.n = n_probe;
-  BankT<double>& b0 = c->bd[0].b;
-  S.x = b0.x; S.y = b0.y; S.z = b0.z; S.ux = b0.ux; S.uy = b0.uy; S.uz = b0.uz; S.E = b0.E; S.w = b0.w;
-  S.w2 = b0.w2; S.rng = b0.rng; S.hid = b0.hid; S.fam = b0.fam; S.probv = nullptr; S.out_off = 0; S.st = c->st;
-  launch_sources(S, c->stream);
-  if (mixed) k_bank_d2f<<<grid_for(n_probe), 256, 0, c->stream>>>(b0, c->bf[0].b, 0, n_probe);
+  sample_bank0(c, S, mixed, false);
   if ((rc = check_state(c)) != ABX_OK) return rc;
   const int block0 = c->block, grid0 = c->grid;
   int best_block = block0, best_grid = grid0;
@@ -1928,11 +1933,7 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
   S.prob = 0;
   S.first_hid = 0;
   S.n = N;
-  BankT<double>& b0 = c->bd[0].b;
-  S.x = b0.x; S.y = b0.y; S.z = b0.z; S.ux = b0.ux; S.uy = b0.uy; S.uz = b0.uz; S.E = b0.E; S.w = b0.w;
-  S.w2 = b0.w2; S.rng = b0.rng; S.hid = b0.hid; S.fam = b0.fam; S.probv = nullptr; S.out_off = 0; S.st = c->st;
-  launch_sources(S, c->stream);
-  if (mixed) k_bank_d2f<<<grid_for(N), 256, 0, c->stream>>>(b0, c->bf[0].b, 0, N);
+  sample_bank0(c, S, mixed, false);
   {
     // RunAcc.global_hist = N; DevState: n_hist = N, kcol = 1, converged
     RunAcc ra{};
@@ -2056,11 +2057,7 @@ extern "C" int abx_run_fixed_source(abx_ctx* c, int nbatches, uint64_t npart, ab
     S.prob = 0;
     S.first_hid = hc;
     S.n = npart;
-    BankT<double>& b0 = c->bd[0].b;
-    S.x = b0.x; S.y = b0.y; S.z = b0.z; S.ux = b0.ux; S.uy = b0.uy; S.uz = b0.uz; S.E = b0.E; S.w = b0.w;
-    S.w2 = b0.w2; S.rng = b0.rng; S.hid = b0.hid; S.fam = b0.fam; S.probv = nullptr; S.out_off = 0; S.st = c->st;
-    launch_sources(S, c->stream);
-    if (mixed) k_bank_d2f<<<grid_for(npart), 256, 0, c->stream>>>(b0, c->bf[0].b, 0, npart);
+    sample_bank0(c, S, mixed, false);
     hc += npart;
     k_step_begin<<<1, 1, 0, c->stream>>>(c->st, npart, 1.0, 1, 0);
     cudaEventRecord(evs[2 * (g - 1)], c->stream);
@@ -2317,15 +2314,11 @@ extern "C" int abx_run_fixed_source_batch(abx_ctx* c, int nbatches, abx_problem_
   SourceArgs S{};
   S.T = TV;
   S.n = total;
-  BankT<double>& b0 = c->bd[0].b;
-  S.x = b0.x; S.y = b0.y; S.z = b0.z; S.ux = b0.ux; S.uy = b0.uy; S.uz = b0.uz; S.E = b0.E; S.w = b0.w;
-  S.w2 = b0.w2; S.rng = b0.rng; S.hid = b0.hid; S.fam = b0.fam; S.probv = b0.prob; S.out_off = 0; S.st = c->st;
   S.seg_off = c->seg_off;
   S.seg_prob = c->seg_prob;
   S.seg_hid0 = c->seg_hid0;
   S.nseg = (int)nv;
-  launch_sources(S, c->stream);
-  if (mixed) k_bank_d2f<<<grid_for(total), 256, 0, c->stream>>>(b0, c->bf[0].b, 0, total);
+  sample_bank0(c, S, mixed, true);
   k_step_begin<<<1, 1, 0, c->stream>>>(c->st, total, 1.0, 1, 0);
   cudaEventRecord(ev[1], c->stream);
   c->batch_tables = TV;

@@ -15,8 +15,9 @@ struct SourceArgs {
   int prob;                 // problem index whose sources are sampled
   uint64_t first_hid;
   uint64_t n;
-  // output bank (double SoA)
+  // output bank (double SoA; the FP32 sampler writes the float arrays)
   double *x, *y, *z, *ux, *uy, *uz, *E, *w, *w2;
+  float *fx, *fy, *fz, *fux, *fuy, *fuz, *fE, *fw, *fw2;
   uint64_t* rng;
   uint64_t* hid;
   uint64_t* fam;
@@ -36,6 +37,7 @@ struct SourceArgs {
 void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace, int grid, int block,
                         cudaStream_t s);
 void launch_sources(const SourceArgs& A, cudaStream_t s);
+void launch_sources_f(const SourceArgs& A, cudaStream_t s);  // transport_mixed.cu
 int transport_regs_d(int tracking);
 
 // transport_mixed.cu (+ transport_mixed_surface.cu); `iso`: every material

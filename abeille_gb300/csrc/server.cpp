@@ -106,13 +106,15 @@ struct ProblemCopy {
     return n;
   }
   // Device bytes while the request runs with `nb` batches: a per-batch FP64
-  // copy of every tally bin plus the average and variance, the double and
-  // float banks and sort counters for all its histories, and the tables
-  // (four copies of the cross-section data covers the derived CDFs, angle
-  // tables and FP32 mirrors).
-  uint64_t footprint(int nb) const {
+  // copy of every tally bin plus the average and variance, the two banks of
+  // the transport precision (nine reals, three 64-bit words and a problem
+  // index per history: 64 B in FP32, 100 B in FP64) and two sort counters
+  // for all its histories, and the tables (four copies of the cross-section
+  // data covers the derived CDFs, angle tables and FP32 mirrors).
+  uint64_t footprint(int nb, bool mixed) const {
     const uint64_t hist = (uint64_t)(p.settings.nparticles > 0 ? p.settings.nparticles : 0) * (uint64_t)nb;
-    return 8 * ((uint64_t)nb + 2) * tally_bins() + 176 * hist + 32 * (uint64_t)mg.size() +
+    const uint64_t per_hist = 2 * (mixed ? 64 : 100) + 8;
+    return 8 * ((uint64_t)nb + 2) * tally_bins() + per_hist * hist + 32 * (uint64_t)mg.size() +
            16 * (uint64_t)(surf.size() + cells.size() + rpn.size() + univ.size() + lat.size()) + (64u << 10);
   }
 };
@@ -394,7 +396,7 @@ extern "C" int abx_server_submit(abx_server* s, const abx_problem* problem, uint
   Request q;
   q.prob.reset(new ProblemCopy());
   q.prob->copy_from(*problem);
-  q.footprint = q.prob->footprint(s->opt.nbatches);
+  q.footprint = q.prob->footprint(s->opt.nbatches, s->opt.precision == ABX_PREC_MIXED);
   q.tag = tag;
   if (q.footprint > s->opt.hbm_budget_bytes)
     return srv_fail(ABX_ERR_BUDGET, "request needs ~%llu bytes, budget %llu", (unsigned long long)q.footprint,

@@ -5,6 +5,7 @@
 // transport_mixed_surface.cu so the two compile in parallel.
 #include "transport_loop.cuh"
 #include "launch.h"
+#include "sources.cuh"
 
 namespace abx {
 
@@ -32,6 +33,13 @@ int occupancy_f(int tracking, bool iso, int block) {
   if (iso) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<float, ABX_TRACK_DELTA, true>, block, 0);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<float, ABX_TRACK_DELTA, false>, block, 0);
   return nb;
+}
+
+void launch_sources_f(const SourceArgs& A, cudaStream_t s) {
+  if (A.n == 0) return;
+  uint64_t blocks = (A.n + 127) / 128;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  sources_kernel<float><<<(unsigned)blocks, 128, 0, s>>>(A);
 }
 
 int transport_regs_f(int tracking) {
