@@ -344,6 +344,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
     }
 
     // --------------------------------------------------------------- descend
+    // Every phase starts at an explicit warp reconvergence point: the lanes
+    // that arrive from different branches of the previous phase run it
+    // together (measured faster than the compiler's own reconvergence).
+    __syncwarp();
     if (ph == PH_WAIT) {
       // CellUniverse/RectLattice::get_cell: re-descent from the first invalid
       // pad, or from the root (restart_get_current) when that fails or when the
@@ -365,6 +369,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
     }
 
     // ------------------------------------------------ post-descend checks
+    __syncwarp();
     if (ph == PH_START) {
       if (k.cell < 0) {  // lost at birth: a warning in the reference, the particle is killed
         ABX_LOST();
@@ -412,6 +417,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
     }
 
     // ----------------------------------------------------------------- moved
+    __syncwarp();
     if (ph == PH_MOVED) {
       if (k.cell < 0 && (TRACK == ABX_TRACK_DELTA || TRACK == ABX_TRACK_CARTER)) {
         // flew out of the geometry: back to the last position, find the
@@ -490,6 +496,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
     }
 
     // --------------------------------------------------------------- collide
+    __syncwarp();
     if (ph == PH_COLL) {
       const ProbT& P = T.probs[L.pid];
       bool alive = true;
@@ -508,6 +515,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
     }
 
     // ------------------------------------------------------------------ dead
+    __syncwarp();
     if (ph == PH_DEAD) {
       if (L.nsec > 0) {
         // Particle::resurect (include/simulation/particle.hpp:170-182)
