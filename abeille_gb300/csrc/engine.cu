@@ -1460,9 +1460,10 @@ extern "C" int abx_transport(abx_ctx* c, const abx_particle* bank, size_t n, dou
 // ------------------------------------------------------------- autotuner
 // Picks the transport launch shape (threads per block, resident blocks per
 // SM) by timing the problem's own first-generation bank: `n_probe` source
-// histories are sampled once, then transported once per candidate (the same
-// histories each time, so every candidate does identical work) and the
-// fastest shape is kept for the context.  Results do not depend on the shape.
+// histories are sampled once, then transported three times per candidate
+// (the same histories each time, so every candidate does identical work;
+// tallies scored as in active generations; the first run warms the caches)
+// and the shape with the fastest run is kept for the context.  Results do not depend on the shape.
 extern "C" int abx_autotune(abx_ctx* c, size_t n_probe, int* block_out, int* grid_out, double* best_ms) {
   if (!c || n_probe == 0 || n_probe > 0xffffffffull) return fail(ABX_ERR_INVALID, "bad arguments");
   if (c->prob0.src_count <= 0) return fail(ABX_ERR_INVALID, "problem has no sources");
@@ -1481,6 +1482,13 @@ extern "C" int abx_autotune(abx_ctx* c, size_t n_probe, int* block_out, int* gri
   S.n = n_probe;
   sample_bank0(c, S, mixed, false);
   if ((rc = check_state(c)) != ABX_OK) return rc;
+  // The probes score the problem's tallies, as active generations do, into a
+  // scratch copy of the tally bins: the context's own bins stay untouched.
+  double* probe_bins = nullptr;
+  const size_t nbins = (size_t)std::max<int64_t>(c->P.tally_bins, 0);
+  if (nbins && nbins <= (size_t(1) << 27)) CUDA_TRY(cudaMalloc(&probe_bins, nbins * 8));
+  std::swap(c->tally_gen, probe_bins);
+  const int converged = c->tally_gen != nullptr && nbins ? 1 : 0;
   const int block0 = c->block, grid0 = c->grid;
   int best_block = block0, best_grid = grid0;
   float best = -1.f;
@@ -1491,13 +1499,15 @@ extern "C" int abx_autotune(abx_ctx* c, size_t n_probe, int* block_out, int* gri
       c->grid = c->nsm * per_sm;
       if ((rc = ensure_sec(c, mixed)) != ABX_OK) break;
       float ms = 0.f;
-      for (int rep = 0; rep < 2; rep++) {  // the first run warms the caches
-        k_step_begin<<<1, 1, 0, c->stream>>>(c->st, n_probe, 1.0, 0, 0);
-        CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+      for (int rep = 0; rep < 3; rep++) {  // the first run warms the caches; the faster of two counts
+        k_step_begin<<<1, 1, 0, c->stream>>>(c->st, n_probe, 1.0, converged, 0);
+        if (cudaEventRecord(c->ev0, c->stream) != cudaSuccess) { rc = fail(ABX_ERR_CUDA, "event record"); break; }
         if ((rc = launch_transport(c, mixed, 0, keig ? scap : 0)) != ABX_OK) break;
-        CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+        if (cudaEventRecord(c->ev1, c->stream) != cudaSuccess) { rc = fail(ABX_ERR_CUDA, "event record"); break; }
         if ((rc = check_state(c)) != ABX_OK) break;
-        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, c->ev0, c->ev1);
+        if (rep == 1 || (rep == 2 && t < ms)) ms = t;
       }
       if (rc) break;
       if (best < 0.f || ms < best) {
@@ -1508,6 +1518,8 @@ extern "C" int abx_autotune(abx_ctx* c, size_t n_probe, int* block_out, int* gri
     }
     if (rc) break;
   }
+  std::swap(c->tally_gen, probe_bins);
+  if (probe_bins) cudaFree(probe_bins);
   c->block = rc ? block0 : best_block;
   c->grid = rc ? grid0 : best_grid;
   if (rc) return rc;

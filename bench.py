@@ -220,8 +220,9 @@ def main():
     ap.add_argument("--rates", default="200,1000,5000", help="config 4: Poisson arrival rates, requests/s")
     ap.add_argument("--duration", type=float, default=3.0, help="config 4: seconds of arrivals per rate")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="config 4: HBM admission budget")
-    ap.add_argument("--autotune", type=int, default=200000,
-                    help="configs 0-2: tune the transport launch shape on this many source histories first (0: off)")
+    ap.add_argument("--autotune", type=int, default=-1,
+                    help="configs 0-2: tune the transport launch shape on this many source histories first "
+                         "(-1: one generation's histories; 0: off)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -244,7 +245,7 @@ def main():
 
     shape = None
     if args.autotune:
-        shape = eng.autotune(args.autotune)
+        shape = eng.autotune(npart if args.autotune < 0 else args.autotune)
     # L2 flush between generations, outside each generation's timed events
     from abeille_gb300 import abi as _abi
     _abi.check(eng.lib.abx_set_l2_flush(eng.ctx, L2_FLUSH_BYTES), eng.lib)

@@ -504,10 +504,10 @@ int abx_last_transport_ms(abx_ctx* ctx, double* ms);
 int abx_set_graphs(abx_ctx* ctx, int enabled);
 
 /* Launch-shape autotuner (no reference counterpart): transports the same
- * `n_probe` first-generation source histories once per candidate shape
- * (128 or 256 threads per block, 1 .. the occupancy limit of blocks per SM)
- * and keeps the fastest for the context.  Results do not depend on the shape.
- * Outputs may be NULL. */
+ * `n_probe` first-generation source histories three times per candidate
+ * shape (128 or 256 threads per block, 1 .. the occupancy limit of blocks per
+ * SM), scoring tallies into scratch bins, and keeps the fastest for the
+ * context.  Results do not depend on the shape.  Outputs may be NULL. */
 int abx_autotune(abx_ctx* ctx, size_t n_probe, int* block, int* grid, double* best_ms);
 
 /* Timing hygiene for benchmarks (no reference counterpart): before each
