@@ -411,9 +411,12 @@ ABX_DEV FissionOut fission_dispatch(const TransportArgs<R>& A, const R* chi, con
 // Transporter::collision + branching_collision + russian_roulette +
 // make_fission_neutrons + do_scatter (src/transporter.cpp:35-93, 269-347, 358-487),
 // MGNuclide::sample_scatter / sample_fission (src/mg_nuclide.cpp:442-461, 504-544)
-template <class R, bool ISO>
+// RESYNC reconverges the colliding lanes after the fission block (measured
+// faster with surface tracking only).
+template <class R, bool ISO, bool RESYNC>
 ABX_DEV void collide(const TransportArgs<R>& A, const Tables& T, const View<R>& V, const ProbT& P,
                      Lane<R>& L, Acc<R>& acc, bool converged, R kcol, bool& alive) {
+  const unsigned cmask = RESYNC ? __activemask() : 0u;
   const MatT M = T.mats[L.mat];
   const int G = M.G, g = L.g;
   const R* xs = V.xs + M.xs_off;
@@ -465,6 +468,7 @@ ABX_DEV void collide(const TransportArgs<R>& A, const Tables& T, const View<R>& 
       L.nsec = o.nsec;
     }
   }
+  if (RESYNC) __syncwarp(cmask);
   // implicit capture
   L.w = L.w * (R(1) - (Eabs + R(0)) / Et);
   L.w2 = L.w2 * (R(1) - (Eabs + R(0)) / Et);

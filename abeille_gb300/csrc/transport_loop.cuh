@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
       bool alive = true;
       ncoll++;
       L.hcoll++;
-      collide<R, ISO>(A, T, V, P, L, acc, converged, kcol, alive);
+      collide<R, ISO, TRACK == ABX_TRACK_SURFACE>(A, T, V, P, L, acc, converged, kcol, alive);
       if (sizeof(R) == 4 && !(m_abs(L.u.x) <= R(1) && m_abs(L.u.y) <= R(1) && m_abs(L.u.z) <= R(1))) {
         // mixed mode: a direction that is not finite cannot be tracked
         ABX_LOST();
