@@ -346,6 +346,7 @@ static int append_problem(Pools& P, const abx_problem* pr) {
       xs[XS_ES * G + g] = es;
       for (int o = 0; o < G; o++) row[o] = sct[(size_t)g * G + o] / es;
       discrete_cdf(row.data(), G, cdf + (size_t)g * G);
+      if (!M.fissile) continue;  // no fission neutron is ever sampled: the chi rows stay zero
       double ci = 0.;
       for (int o = 0; o < G; o++) ci += chi[(size_t)g * G + o];
       for (int o = 0; o < G; o++) row[o] = chi[(size_t)g * G + o] / ci;
@@ -355,11 +356,14 @@ static int append_problem(Pools& P, const abx_problem* pr) {
     M.dg_off = (int)P.dg_d.size();
     P.dg_d.resize(P.dg_d.size() + (size_t)std::max(1, mt.n_delayed));
     discrete_cdf(dgp, mt.n_delayed, P.dg_d.data() + M.dg_off);
-    // angle tables
+    // angle tables; none when every Legendre moment is zero (isotropic
+    // scattering, whose flat tables sampling inverts directly)
     const size_t hdr0 = P.ang_hdr.size(), ang0 = P.ang_d.size();
     M.ang_off = (int)hdr0;
     M.iso = 1;
-    for (int gi = 0; gi < G; gi++)
+    bool all_flat = true;
+    for (size_t q = 0, nq = (size_t)mt.n_legendre * G * G; q < nq && all_flat; q++) all_flat = legm[q] == 0.;
+    for (int gi = 0; gi < G && !all_flat; gi++)
       for (int go = 0; go < G; go++) {
         double ac[6] = {0.5, 0., 0., 0., 0., 0.};
         bool flat = true;
@@ -2131,6 +2135,47 @@ void* batch_prepare(const abx_problem* problems, int n_problems, int* rc_out) {
     b->n = n_problems;
     b->tracking = problems[0].settings.tracking;
     b->prec = problems[0].settings.precision;
+    // the pools sized up front: no reallocation while appending
+    size_t nxs = 0, ncdf = 0, nmat = 0, ndg = 0, neb = 0, nsurf = 0, ncell = 0, nrpn = 0, nuniv = 0, nlist = 0,
+           nlat = 0, ntal = 0, nteb = 0, nsrc = 0;
+    auto cnt = [](int v) { return (size_t)std::max(0, v); };
+    for (int i = 0; i < n_problems; i++) {
+      const abx_problem& q = problems[i];
+      const size_t G = cnt(q.settings.ngroups), nm = cnt(q.n_materials);
+      nxs += nm * XS_ROWS * G;
+      ncdf += nm * 2 * G * G;
+      nmat += nm;
+      if (q.materials)
+        for (size_t m = 0; m < nm; m++) ndg += (size_t)std::max(1, q.materials[m].n_delayed);
+      neb += G + 1;
+      nsurf += cnt(q.n_surfaces);
+      ncell += cnt(q.n_cells);
+      nrpn += 2 * cnt(q.n_rpn);  // cell regions and the boundary half-spaces of each universe
+      nuniv += cnt(q.n_universes);
+      nlist += cnt(q.n_cell_lists);
+      nlat += cnt(q.n_lattice_elems);
+      ntal += cnt(q.n_tallies);
+      nteb += cnt(q.n_tally_ebounds);
+      nsrc += cnt(q.n_sources);
+    }
+    Pools& P = b->P;
+    P.xs_d.reserve(nxs);
+    P.cdf_d.reserve(ncdf);
+    P.mats.reserve(nmat);
+    P.dg_d.reserve(ndg);
+    P.eb_d.reserve(neb);
+    P.maj_d.reserve(2 * neb);
+    P.probs.reserve(n_problems);
+    P.surf_d.reserve(nsurf);
+    P.cells.reserve(ncell);
+    P.rpn.reserve(nrpn);
+    P.univ.reserve(nuniv);
+    P.cell_lists.reserve(nlist);
+    P.lat_elems.reserve(nlat);
+    P.tallies.reserve(ntal);
+    P.tally_eb.reserve(nteb);
+    P.sources.reserve(nsrc);
+    P.src_cdf.reserve(nsrc + n_problems);
     for (int i = 0; i < n_problems && rc == ABX_OK; i++) {
       const abx_settings& s = problems[i].settings;
       if (s.mode != ABX_MODE_FIXED_SOURCE || s.tracking != b->tracking || s.precision != b->prec)

@@ -88,6 +88,15 @@ class Engine:
                                           C.byref(g)))
         return {"gen": gen, "avg": avg, "var": var, "generations": g.value}
 
+    def tally_all(self):
+        """Average and variance of every tally bin of the context (in a batch
+        context: every problem's bins, problem after problem), in one read."""
+        n = C.c_size_t()
+        self._chk(self.lib.abx_tally_read_all(self.ctx, None, None, 0, C.byref(n)))
+        avg, var = np.empty(n.value), np.empty(n.value)
+        self._chk(self.lib.abx_tally_read_all(self.ctx, avg.ctypes.data, var.ctypes.data, n.value, C.byref(n)))
+        return avg, var
+
     def record_generation(self, multiplier=1.0):
         self._chk(self.lib.abx_tally_record_generation(self.ctx, multiplier))
 

@@ -335,24 +335,32 @@ def bench_batch(args):
     builts = [b.build(precision=args.precision) for b in builders]
     hist_per_step = nb * sum(b.nparticles for b in builders)
 
-    # end to end, once: create (host tables + upload) + run + every tally read back
+    # the context, created once (its CUDA set-up is not part of a step)
     t0 = time.perf_counter()
     eng = BatchEngine(builts, local)
-    t_create = time.perf_counter() - t0
-    t1 = time.perf_counter()
-    rows, st_e = eng.run(nb)
-    t_run = time.perf_counter() - t1
-    t2 = time.perf_counter()
-    d2h = 0
-    for r in rows:
-        t = eng.tally(r["tally_first"])
-        d2h += t["avg"].nbytes + t["var"].nbytes + t["gen"].nbytes
-    t_read = time.perf_counter() - t2
-    e2e_wall = t_create + t_run + t_read
-    e2e_coll = st_e["collisions"]
-    h2d = sum(sum(getattr(a, "nbytes", 0) for a in b._keep) for b in builts)
-    for _ in range(max(args.warmup - 1, 0)):
+    t_first = time.perf_counter() - t0
+    for _ in range(max(args.warmup, 1)):
         eng.run(nb)
+    # end to end, every step: the problems' tables from host memory
+    # (abx_batch_replace: host preparation + upload), the run, and the
+    # average and variance of every tally bin read back
+    t_load = t_run = t_read = 0.0
+    e2e_coll = 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        eng.replace(builts)
+        t1 = time.perf_counter()
+        rows, st_e = eng.run(nb)
+        t2 = time.perf_counter()
+        avg, var = eng.tally_all()  # every problem's bins, problem after problem
+        t3 = time.perf_counter()
+        t_load += t1 - t0
+        t_run += t2 - t1
+        t_read += t3 - t2
+        e2e_coll += st_e["collisions"]
+    e2e_wall = t_load + t_run + t_read
+    d2h = avg.nbytes + var.nbytes
+    h2d = sum(sum(getattr(a, "nbytes", 0) for a in b._keep) for b in builts)
     if dist:
         dist.barrier()
     coll = flights = 0
@@ -408,12 +416,16 @@ def bench_batch(args):
         "roofline": roof, "cpu_baseline": cpu,
         "e2e": {"value": e2e_coll / e2e_wall, "unit": "collisions/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "what": "abx_create_batch + abx_run_fixed_source_batch + every tally read back, wall"},
+                "what": "per step: abx_batch_replace (host tables + upload) + abx_run_fixed_source_batch + "
+                        "abx_tally_read_all (average and variance of every bin), wall"},
         "per_problem_launch": per,
-        "gpu_launches": (8 if args.precision == "mixed" else 7) * args.steps,
+        # per step: zero the batch tallies, sample, step begin, transport,
+        # batch tally record, problem record, generation end
+        "gpu_launches": 7 * args.steps,
         "clocks": clk.summary(),
-        "detail": {"collisions": coll, "flights": flights, "transport_ms": tr_ms, "create_s": t_create,
-                   "run_wall_s": t_run, "tally_read_s": t_read,
+        "detail": {"collisions": coll, "flights": flights, "transport_ms": tr_ms, "first_create_s": t_first,
+                   "e2e_load_s": t_load / args.steps, "e2e_run_s": t_run / args.steps,
+                   "e2e_tally_read_s": t_read / args.steps,
                    "lost": int(sum(r["lost"] for r in rows))},
     }
     print(json.dumps(line), flush=True)
@@ -562,9 +574,9 @@ def bench_server(args):
 
 
 # DRAM bytes (read + write) per history of a transport launch, from the ncu
-# capture in profiles/transport_kernel_config1_mixed_300k.md (274.2 MB at
+# capture in profiles/transport_kernel_config1_mixed_300k.md (157.6 MB at
 # 300,000 histories); bank, site and spill traffic grow with the histories.
-TRAFFIC_PER_HISTORY = {(1, "mixed"): 274.21e6 / 3e5}
+TRAFFIC_PER_HISTORY = {(1, "mixed"): 157.60e6 / 3e5}
 L2_FLUSH_BYTES = 256 << 20
 
 if __name__ == "__main__":

@@ -51,6 +51,11 @@ def test_batch_matches_oracle_per_problem():
         tg, tc = eng.tally(r["tally_first"]), o.tally(0)
         assert tg["generations"] == tc["generations"] == NBATCH
         assert np.allclose(tg["avg"], tc["avg"], rtol=1e-10, atol=0), p
+    # one read of every bin: the problems' tallies one after the other
+    avg_all, var_all = eng.tally_all()
+    per = [eng.tally(r["tally_first"]) for r in rows]
+    assert np.array_equal(avg_all, np.concatenate([t["avg"] for t in per]))
+    assert np.array_equal(var_all, np.concatenate([t["var"] for t in per]))
     eng.close()
 
 
