@@ -223,9 +223,14 @@ def main():
     ap.add_argument("--autotune", type=int, default=-1,
                     help="configs 0-2: tune the transport launch shape on this many source histories first "
                          "(-1: one generation's histories; 0: off)")
+    ap.add_argument("--zscore", type=int, default=0,
+                    help="config 1: compare mixed and FP64 over sets of this many replicas instead of timing")
+    ap.add_argument("--zsets", type=int, default=1, help="with --zscore: replica sets per precision")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.zscore:
+        return bench_zscore(args)
     if args.config == 3:
         return bench_batch(args)
     if args.config == 4:
@@ -455,6 +460,67 @@ def _per_problem_launch(idx, nb, precisions, device, tracking=None):
         per[prec] = {"value": c_sum / wall, "transport_only_value": c_sum / dev, "unit": "collisions/s",
                      "problems": len(idx), "precision": prec}
     return per
+
+
+def bench_zscore(args):
+    """Mixed against FP64 on config 1 over independent replicas: `--zsets` S
+    sets of `--zscore` R replicas per precision (own seed each; `--particles`
+    histories per generation, default 1e5, 10 inactive + 40 active
+    generations).  Every pair of sets is compared: k difference in sigma and
+    the fraction of flux bins with |z| < 2, sigma of each mean from the
+    replica spread.  With R replicas per set the z of two identical
+    distributions follows a Student t with about 2(R-1) degrees of freedom
+    (the expected fraction is printed), and because all bins share one
+    fission source the fraction moves by a percent or more from one pair of
+    sets to another: FP64/FP64 pairs show that spread."""
+    import itertools
+
+    import __graft_entry__
+    __graft_entry__.build()
+    import numpy as np
+    from scipy import stats as _st
+    from abeille_gb300 import Engine, decks
+
+    R, S = args.zscore, max(args.zsets, 1)
+    npart = args.particles or 100000
+    sets = {}
+    t0 = time.perf_counter()
+    for si in range(S):
+        for prec in ("fp64", "mixed"):
+            ks, avgs = [], []
+            for rep in range(R):
+                b = decks.config1(nparticles=npart)
+                b.seed = 20000 + 100000 * si + (50000 if prec == "mixed" else 0) + rep
+                eng = Engine(b.build(precision=prec), 0)
+                st, _, _ = eng.run_power_iteration(50, 10)
+                ks.append(st["kcol_avg"])
+                avgs.append(eng.tally(0)["avg"])
+                eng.close()
+            sets[f"{prec}{si + 1}"] = (np.array(ks), np.array(avgs))
+
+    pairs = []
+    for x, y in itertools.combinations(sorted(sets), 2):
+        (kx, ax), (ky, ay) = sets[x], sets[y]
+        dk = (kx.mean() - ky.mean()) / np.sqrt(kx.var(ddof=1) / R + ky.var(ddof=1) / R)
+        keep = (ax.mean(0) > 0) & (ay.mean(0) > 0)
+        z = ((ax.mean(0) - ay.mean(0)) / np.sqrt(ax.var(0, ddof=1) / R + ay.var(0, ddof=1) / R))[keep]
+        kind = "mixed/fp64" if x[:2] != y[:2] else ("fp64/fp64" if x.startswith("fp64") else "mixed/mixed")
+        pairs.append({"pair": f"{x} {y}", "kind": kind, "dk_sigma": round(float(dk), 3), "bins": int(keep.sum()),
+                      "frac_abs_z_lt_2": round(float(np.mean(np.abs(z) < 2)), 4), "mean_z": round(float(z.mean()), 4)})
+    dof = 2 * (R - 1)
+    summ = {}
+    for kind in ("fp64/fp64", "mixed/fp64", "mixed/mixed"):
+        f = [p["frac_abs_z_lt_2"] for p in pairs if p["kind"] == kind]
+        if f:
+            summ[kind] = {"pairs": len(f), "frac_min": min(f), "frac_max": max(f), "frac_mean": round(float(np.mean(f)), 4)}
+    line = {"metric": "mixed vs fp64 agreement", "workload": WORKLOADS[1], "replicas_per_set": R, "sets_per_precision": S,
+            "histories_per_generation": npart, "generations": "10 inactive + 40 active",
+            "k_mixed": float(np.mean([sets[k][0].mean() for k in sets if k.startswith("mixed")])),
+            "k_fp64": float(np.mean([sets[k][0].mean() for k in sets if k.startswith("fp64")])),
+            "frac_expected_identical": round(float(_st.t.cdf(2, dof) - _st.t.cdf(-2, dof)), 4),
+            "summary": summ, "pairs": pairs, "wall_s": round(time.perf_counter() - t0, 1)}
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def bench_server(args):
