@@ -143,9 +143,9 @@ ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& ac
 
 // Occupancy (measured on config 1 and config 2): FP32 delta tracking (and
 // implicit-leakage delta tracking) runs four 256-thread blocks per SM (64
-// registers), FP32 surface tracking three (80 registers), FP64 two (128).
+// registers), FP32 surface tracking three (80 registers), FP64 three (80).
 template <class R, int TRACK, bool ISO>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURFACE ? 4 : 3) : 2)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURFACE ? 4 : 3) : 3)
     transport_kernel(const __grid_constant__ TransportArgs<R> A) {
   const bool TRACE = A.trace != nullptr;
   const Tables& T = A.T;
