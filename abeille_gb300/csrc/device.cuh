@@ -734,7 +734,8 @@ template <class R> ABX_DEV Bound<R> trk_nearest(const Tables& T, const View<R>& 
 // then taken from the token and c = 0 exactly: FP32 rounding of c would
 // otherwise put a particle that just crossed outward back inside, and the
 // next flight would cross again at distance 0, back and forth.
-template <class R> ABX_DEV R exit_dist(const SurfT<R>& s, int32_t t, V3<R> r, V3<R> u, bool on_it) {
+template <class R, bool FAST32 = false>
+ABX_DEV R exit_dist(const SurfT<R>& s, int32_t t, V3<R> r, V3<R> u, bool on_it) {
   const R INF = Tol<R>::INF;
   if (s.type <= ABX_SURF_PLANE) {
     R eval = surf_eval(s, r);
@@ -768,8 +769,31 @@ template <class R> ABX_DEV R exit_dist(const SurfT<R>& s, int32_t t, V3<R> r, V3
     return d > R(0) ? d : R(0);
   }
   if (a == R(0)) return ((t < 0) == (c > R(0))) ? R(0) : INF;
-  // roots of a s^2 + 2 k s + c = 0; FP64 when the discriminant is small
-  // against k^2 (grazing incidence), where FP32 cancellation would dominate
+  // roots of a s^2 + 2 k s + c = 0.  With FAST32 (the nearest-boundary search
+  // of surface tracking) away from grazing incidence in FP32, in the
+  // cancellation-free form: with qq = -(k + sign(k) sqrt(k^2 - a c)) the roots
+  // are qq / a and c / qq.  FP64 otherwise, and always when the discriminant is
+  // small against k^2 (grazing incidence), where FP32 cancellation in
+  // k^2 - a c dominates.  (The boundary-condition search, shared with delta
+  // tracking, keeps the FP64 form: delta tracking measured faster with it.)
+  if (FAST32 && sizeof(R) == 4) {
+    const R quadf = k * k - a * c;
+    if (quadf > R(1e-3) * k * k) {
+      const R sq = m_sqrt(quadf);
+      const R qq = k >= R(0) ? -(k + sq) : sq - k;
+      if (qq != R(0)) {
+        const R lo = qq / a, hi = c / qq;  // k >= 0: lo <= hi; k < 0: the other way round
+        const R nearr = k >= R(0) ? lo : hi, farr = k >= R(0) ? hi : lo;
+        if (t < 0) {  // inside: leave through the far root
+          if (c > R(0) && k >= R(0)) return R(0);
+          return farr > R(0) ? farr : R(0);
+        }
+        if (c < R(0)) return R(0);  // outside region but within the quadric
+        if (k >= R(0)) return INF;
+        return nearr > R(0) ? nearr : R(0);
+      }
+    }
+  }
   double ad = a, kd = k, cd = c;
   double quad = kd * kd - ad * cd;
   if (t < 0) {  // inside: leave through the far root
@@ -786,7 +810,7 @@ template <class R> ABX_DEV R exit_dist(const SurfT<R>& s, int32_t t, V3<R> r, V3
 
 // Distance to leave a simple cell (intersection of half-spaces); for a cell
 // with unions or complements the reference's per-surface distances are used.
-template <class R>
+template <class R, bool FAST32 = false>
 ABX_DEV void cell_exit(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<R> u, int32_t on, bool bc_only,
                        R& dist, int32_t& isurf) {
   const CellT c = T.cells[ci];
@@ -801,7 +825,7 @@ ABX_DEV void cell_exit(const Tables& T, const View<R>& V, int ci, V3<R> r, V3<R>
     int32_t t = __ldg(rpn + i);
     const SurfT<R> s = V.surf[abs(t) - 1];
     if (bc_only && s.bc == ABX_BC_NORMAL) continue;
-    R d = exit_dist(s, t, r, u, t == on);
+    R d = exit_dist<R, FAST32>(s, t, r, u, t == on);
     if (d < mind) { mind = d; is = -t; }
   }
   dist = mind;
@@ -905,7 +929,7 @@ template <class R> ABX_DEV Bound<R> trk_nearest_mixed(const Tables& T, const Vie
         if (d < b.dist && !bc_tie) { b.dist = d; b.btype = ABX_BC_NORMAL; b.si = -1; b.token = 0; }
       } else if (ty == PAD_CELL) {
         R d; int32_t ts;
-        cell_exit(T, V, id, rl, k.u, k.token, false, d, ts);
+        cell_exit<R, true>(T, V, id, rl, k.u, k.token, false, d, ts);
         if (d < b.dist) {
           b.dist = d;
           b.token = -ts;  // the cell's own side: crossing flips it
