@@ -199,6 +199,8 @@ PROTOTYPES = {
     "abx_run_fixed_source_batch": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(ProblemResult), C.POINTER(RunStats)]),
     "abx_batch_replace": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.c_int]),
     "abx_tally_read_all": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "abx_read_source_bank": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t),
+                                       C.POINTER(C.c_double)]),
     "abx_server_create": (C.c_int, [C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
     "abx_server_destroy": (C.c_int, [C.c_void_p]),
     "abx_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.c_uint64, C.POINTER(C.c_uint64)]),

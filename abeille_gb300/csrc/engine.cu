@@ -737,6 +737,11 @@ struct abx_context {
   Tables batch_tables{};
   // captured generation step (one graph per bank parity)
   bool use_graphs = true;
+  // the bank parity holding the next generation's source after a power
+  // iteration (-1: none, or overwritten since), its size and k_col
+  int pi_bank = -1;
+  size_t pi_n = 0;
+  double pi_kcol = 1.;
   cudaGraphExec_t gen_exec[2] = {nullptr, nullptr};
   cudaGraph_t gen_graph[2] = {nullptr, nullptr};  // kept: exec updates name its nodes
   cudaGraphNode_t gen_ev_node[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -1143,6 +1148,7 @@ static int ensure_counts(abx_ctx* c, size_t n) {
 
 static int ensure_banks(abx_ctx* c, size_t n, bool mixed, bool with_prob) {
   int rc;
+  c->pi_bank = -1;  // every caller writes bank 0 next
   // banks of the transport precision only (mixed runs sample in FP32)
   for (int i = 0; i < 2; i++) {
     if (!mixed && (c->bd[i].cap < n || (with_prob && !c->bd[i].b.prob)))
@@ -1995,6 +2001,12 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
   }
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   c->tally_g = active_tally;
+  if (rc == ABX_OK) {
+    // the last check_state read DevState after the final generation end
+    c->pi_bank = cur;
+    c->pi_n = (size_t)c->st_host->n_hist;
+    c->pi_kcol = c->st_host->kcol;
+  }
   double tms = 0.;
   std::vector<abx_gen_record> recs(ngen);
   if (rc == ABX_OK) CUDA_TRY(cudaMemcpy(recs.data(), c->gen_rec, ngen * sizeof(abx_gen_record), cudaMemcpyDeviceToHost));
@@ -2029,6 +2041,31 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
     stats->transport_ms = tms;
     stats->total_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   }
+  return ABX_OK;
+}
+
+extern "C" int abx_read_source_bank(abx_ctx* c, abx_particle* out, size_t capacity, size_t* n_out,
+                                    double* kcol_out) {
+  if (!c || !n_out) return fail(ABX_ERR_INVALID, "bad arguments");
+  if (c->pi_bank < 0) return fail(ABX_ERR_INVALID, "no source bank: no power iteration since the banks were last written");
+  const size_t n = c->pi_n;
+  *n_out = n;
+  if (kcol_out) *kcol_out = c->pi_kcol;
+  if (!out || n == 0) return ABX_OK;
+  if (capacity < n) return fail(ABX_ERR_CAPACITY, "source bank of %zu particles, capacity %zu", n, capacity);
+  cudaSetDevice(c->device);
+  if (c->aos_in_cap < n) {
+    if (c->aos_in) cudaFree(c->aos_in);
+    c->aos_in = nullptr;
+    c->aos_in_cap = 0;
+    CUDA_TRY(cudaMalloc(&c->aos_in, n * sizeof(abx_particle)));
+    c->aos_in_cap = n;
+  }
+  if (mixed_of(c)) k_bank_to_aos<float><<<grid_for(n), 256, 0, c->stream>>>(c->bf[c->pi_bank].b, n, c->aos_in);
+  else k_bank_to_aos<double><<<grid_for(n), 256, 0, c->stream>>>(c->bd[c->pi_bank].b, n, c->aos_in);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(out, c->aos_in, n * sizeof(abx_particle), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
   return ABX_OK;
 }
 

@@ -88,6 +88,15 @@ class Engine:
                                           C.byref(g)))
         return {"gen": gen, "avg": avg, "var": var, "generations": g.value}
 
+    def read_source_bank(self):
+        """(bank, kcol): the source bank the next generation would run after
+        the last power iteration, and the k_col its transport takes."""
+        n, k = C.c_size_t(), C.c_double()
+        self._chk(self.lib.abx_read_source_bank(self.ctx, None, 0, C.byref(n), C.byref(k)))
+        bank = np.zeros(n.value, PARTICLE_DTYPE)
+        self._chk(self.lib.abx_read_source_bank(self.ctx, bank.ctypes.data, n.value, C.byref(n), C.byref(k)))
+        return bank, k.value
+
     def tally_all(self):
         """Average and variance of every tally bin of the context (in a batch
         context: every problem's bins, problem after problem), in one read."""

@@ -170,7 +170,7 @@ def run_reference(args):
     return 0
 
 
-def e2e_measure(eng, bank_np, steps, warmup):
+def e2e_measure(eng, bank_np, kcol, steps, warmup):
     """abx_transport with the bank and the site buffer in pinned host memory."""
     import numpy as np
     import torch
@@ -187,7 +187,7 @@ def e2e_measure(eng, bank_np, steps, warmup):
     coll, secs, h2d, d2h = 0, 0.0, 0, 0
     for i in range(warmup + steps):
         t0 = time.perf_counter()
-        rc = lib.abx_transport(eng.ctx, C.cast(pin_b.data_ptr(), C.POINTER(abi.Particle)), n, 1.0, 1,
+        rc = lib.abx_transport(eng.ctx, C.cast(pin_b.data_ptr(), C.POINTER(abi.Particle)), n, kcol, 1,
                                C.cast(pin_s.data_ptr(), C.POINTER(abi.Site)), cap, C.byref(ns), C.byref(sc))
         dt = time.perf_counter() - t0
         abi.check(rc, lib)
@@ -272,8 +272,10 @@ def main():
 
     e2e = None
     if not args.no_e2e:
-        bank = eng.sample_sources(0, npart)
-        v, h2d, d2h = e2e_measure(eng, bank, max(2, args.steps // 3), 1)
+        # the bank of the generation after the timed ones (the converged
+        # source, the same workload as the timed generations)
+        bank, kcol = eng.read_source_bank()
+        v, h2d, d2h = e2e_measure(eng, bank, kcol, max(2, args.steps // 3), 1)
         e2e = {"value": v * world, "unit": "collisions/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     if rank != 0:

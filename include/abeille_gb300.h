@@ -363,6 +363,19 @@ typedef struct abx_gen_record {
 int abx_run_power_iteration_ex(abx_ctx* ctx, int ngenerations, int nignored,
                                abx_run_stats* stats, abx_gen_record* per_gen);
 
+/* The source bank the next generation would run after the last
+ * abx_run_power_iteration[_ex] of the context: the reference's `bank` at
+ * the end of PowerIterator::run (src/power_iterator.cpp:396-404, fission
+ * sites turned into particles: normalised weights, new history ids, re-seeded
+ * streams), which it can also write out as a source file
+ * (src/simulation.cpp:137-175).  *n_out is its size; with out == NULL only
+ * the size is returned.  *kcol_out (may be NULL) is the last generation's
+ * k_col, the `kcol` a transport of this bank takes.  ABX_ERR_INVALID when no
+ * power iteration ran since the banks were last written by another call
+ * (transport, source sampling, fixed-source runs, the autotuner). */
+int abx_read_source_bank(abx_ctx* ctx, abx_particle* out, size_t capacity,
+                         size_t* n_out, double* kcol_out);
+
 /* FixedSource::run (src/fixed_source.cpp:81-173). */
 int abx_run_fixed_source(abx_ctx* ctx, int nbatches, uint64_t nparticles,
                          abx_run_stats* stats);

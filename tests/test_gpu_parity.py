@@ -113,6 +113,49 @@ def test_power_iteration_matches():
     assert np.allclose(tg["avg"], tc["avg"], rtol=1e-10, atol=0)
 
 
+def _pcg_start(seed, stride, hid):
+    """pcg32 state of history `hid`: seeded on the default stream, then
+    advanced stride * hid steps (the LCG jump-ahead by squaring)."""
+    M, INC, MASK = 6364136223846793005, 1442695040888963407, (1 << 64) - 1
+    state = ((seed + INC) * M + INC) & MASK
+    delta, am, ap, cm, cp = (stride * hid) & MASK, 1, 0, M, INC
+    while delta:
+        if delta & 1:
+            am, ap = (am * cm) & MASK, (ap * cm + cp) & MASK
+        cp, cm = ((cm + 1) * cp) & MASK, (cm * cm) & MASK
+        delta >>= 1
+    return (am * state + ap) & MASK
+
+
+def test_source_bank_after_power_iteration():
+    """The bank the next generation would run (PowerIterator's `bank` after
+    its loop): consecutive history ids after every history already run,
+    weights normalised to N in total, each stream re-seeded at its history id,
+    the last k_col; a transport of it matches the oracle's transport of the
+    same bank, and that transport replaces it."""
+    b = decks.config0(nparticles=2000)
+    eng, ora, _ = pair(b, nthreads=oracle.cores())
+    st, kc, _ = eng.run_power_iteration(4, 1)
+    bank, kcol = eng.read_source_bank()
+    assert kcol == kc[-1]
+    n = len(bank)
+    assert n > 0
+    ids = bank["history_id"]
+    assert ids[0] == st["histories"] and np.array_equal(ids, np.arange(ids[0], ids[0] + n))
+    assert abs(bank["wgt"].sum() - 2000.0) <= 1e-9 * 2000.0
+    for i in (0, 1, n - 1):  # pcg32 seeded, then advanced stride * history id (particle.hpp:188-193)
+        assert int(bank["rng_state"][i]) == _pcg_start(b.seed, b.stride, int(ids[i]))
+    sg, cg = eng.transport(bank, kcol, True)
+    sc, cc = ora.transport(bank, kcol, True)
+    assert np.array_equal(sg["parent_history_id"], sc["parent_history_id"])
+    assert np.array_equal(sg["parent_daughter_id"], sc["parent_daughter_id"])
+    assert close(sg["r"], sc["r"], atol=1e-9)
+    for k in ("collisions", "flights", "lost"):
+        assert cg[k] == cc[k], k
+    with pytest.raises(AbxError):
+        eng.read_source_bank()
+
+
 def test_fixed_source_matches():
     b = decks.fixed_source_problem(0, nparticles=3000, precision="fp64")
     eng, ora, _ = pair(b, nthreads=oracle.cores())
