@@ -1,6 +1,6 @@
 """In-tree build of the CUDA engine (sm_103a) into abeille_gb300/_lib/.
 
-Six translation units are compiled in parallel with nvcc and linked into one
+Seven translation units are compiled in parallel with nvcc and linked into one
 shared library exposing the C-ABI of include/abeille_gb300.h:
 
   engine.cu                   host side + bookkeeping kernels     --fmad=false
@@ -34,6 +34,7 @@ UNITS = [
     ("transport_mixed.cu", []),
     ("transport_mixed_surface.cu", []),
     ("transport_mixed_variants.cu", []),
+    ("transport_mixed_branchless.cu", []),
     ("server.cpp", []),
 ]
 

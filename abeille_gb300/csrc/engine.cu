@@ -477,6 +477,17 @@ static int append_problem(Pools& P, const abx_problem* pr) {
   pt.wgt_split_f = (float)pt.wgt_split;
   if (s.tracking == ABX_TRACK_CARTER && !(pt.wgt_split > s.wgt_survival))
     return fail(ABX_ERR_INVALID, "wgt-split must exceed wgt-survival (src/parser.cpp:689-697)");
+  pt.branchless = 0;
+  if (s.branchless) {
+    if (s.branchless & ~(ABX_BRANCHLESS_ON | ABX_BRANCHLESS_MATERIAL | ABX_BRANCHLESS_SPLITTING) ||
+        !(s.branchless & ABX_BRANCHLESS_ON))
+      return fail(ABX_ERR_INVALID, "branchless flags %d", s.branchless);
+    if (s.mode != ABX_MODE_K_EIGENVALUE)
+      return fail(ABX_ERR_UNSUPPORTED, "branchless collisions belong to the branchless k-eigenvalue simulation");
+    if (s.tracking != ABX_TRACK_DELTA && s.tracking != ABX_TRACK_SURFACE)
+      return fail(ABX_ERR_UNSUPPORTED, "branchless collisions with delta or surface tracking only");
+    pt.branchless = s.branchless;
+  }
   pt.nparticles = s.nparticles;
   pt.inv_np = 1. / s.nparticles;
   pt.min_energy = std::max(0., pr->energy_bounds[0]);  // src/parser.cpp:157-168
@@ -806,6 +817,7 @@ __global__ void k_step_begin(DevState* st, unsigned long long n, double kcol, in
   st->site_count = 0;
   st->site_pos = 0;
   st->site_neg = 0;
+  st->site_wsum = 0.;
   st->collisions = 0;
   st->flights = 0;
   st->lost = 0;
@@ -890,7 +902,9 @@ __global__ void k_next_bank(SiteT<R> S, DevState* st, const uint32_t* off, BankT
                             const ProbT* probs, RunAcc* run, uint64_t cap, double* ent_bins, double* ent_total) {
   const unsigned long long ns = st->site_count;
   const ProbT& P = probs[0];
-  const double W = (double)st->site_pos - (double)st->site_neg;
+  // normalize_weights (src/power_iterator.cpp:538-586): N over the bank's net
+  // weight, sites of weight +-1 unless the collisions are branchless
+  const double W = P.branchless ? st->site_wsum : (double)st->site_pos - (double)st->site_neg;
   const double wpp = P.nparticles / W;
   const unsigned long long g0 = run->global_hist;
   double w_in_mesh = 0.;  // this thread's share of the entropy total
@@ -1171,13 +1185,19 @@ static int ensure_sites(abx_ctx* c, size_t n, bool mixed) {
 
 static int ensure_sec(abx_ctx* c, bool mixed) {
   // secondaries: fission in fixed-source problems, splitting in Carter tracking
-  const bool carter = c->prob0.tracking == ABX_TRACK_CARTER;
+  // splitting (Carter tracking, branchless collisions) needs the stack in
+  // every mode
+  const bool bl_split = (c->prob0.branchless & ABX_BRANCHLESS_SPLITTING) != 0;
+  const bool carter = c->prob0.tracking == ABX_TRACK_CARTER || bl_split;
   if (!carter && (c->prob0.mode != ABX_MODE_FIXED_SOURCE || !c->fissile_any)) return ABX_OK;
-  if (carter && c->sec_cap < 64) {
+  // branchless splitting piles copies up within a history (the oracle saw
+  // 190 pending copies in 2e6 histories of the critical slabs)
+  const uint32_t want = bl_split ? 512 : 64;
+  if (carter && c->sec_cap < want) {
     if (c->sec) cudaFree(c->sec);
     c->sec = nullptr;
     c->sec_threads = 0;
-    c->sec_cap = 64;
+    c->sec_cap = want;
   }
   size_t threads = (size_t)c->grid * c->block;
   size_t need = threads * c->sec_cap * 9 * (mixed ? sizeof(float) : sizeof(double));
@@ -1205,6 +1225,11 @@ static int check_state(abx_ctx* c) {
   return ABX_OK;
 }
 
+// which transport kernel: the tracking mode, plus the branchless-collision bit
+static int kernel_code(const abx_ctx* c) {
+  return c->prob0.tracking | (c->prob0.branchless ? ABX_KERNEL_BRANCHLESS : 0);
+}
+
 template <class R> static TransportArgs<R> make_args(abx_ctx* c, const BankT<R>& bank, const SiteT<R>& sites,
                                                      size_t site_cap) {
   TransportArgs<R> A{};
@@ -1229,10 +1254,10 @@ template <class R> static TransportArgs<R> make_args(abx_ctx* c, const BankT<R>&
 static int launch_transport(abx_ctx* c, bool mixed, int which_bank, size_t site_cap) {
   if (mixed) {
     TransportArgs<float> A = make_args<float>(c, c->bf[which_bank].b, c->sf.s, site_cap);
-    launch_transport_f(A, c->prob0.tracking, c->all_iso, c->trace_nhist > 0, c->grid, c->block, c->stream);
+    launch_transport_f(A, kernel_code(c), c->all_iso, c->trace_nhist > 0, c->grid, c->block, c->stream);
   } else {
     TransportArgs<double> A = make_args<double>(c, c->bd[which_bank].b, c->sd.s, site_cap);
-    launch_transport_d(A, c->prob0.tracking, c->trace_nhist > 0, c->grid, c->block, c->stream);
+    launch_transport_d(A, kernel_code(c), c->trace_nhist > 0, c->grid, c->block, c->stream);
   }
   CUDA_TRY(cudaGetLastError());
   return ABX_OK;
@@ -1325,7 +1350,7 @@ static int create_ctx(const abx_problem* problems, int nprob, int device, abx_ct
   int block = problem->settings.block_size > 0 ? problem->settings.block_size : 256;
   block = std::max(32, std::min(256, block / 32 * 32));
   c->block = block;
-  int occ = prec == ABX_PREC_MIXED ? occupancy_f(c->prob0.tracking, c->all_iso, block) : occupancy_d(c->prob0.tracking, block);
+  int occ = prec == ABX_PREC_MIXED ? occupancy_f(kernel_code(c), c->all_iso, block) : occupancy_d(kernel_code(c), block);
   if (occ < 1) occ = 1;
   c->grid = c->nsm * occ;
   if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(ABX_ERR_CUDA, "device sync failed"));
@@ -1503,7 +1528,7 @@ extern "C" int abx_autotune(abx_ctx* c, size_t n_probe, int* block_out, int* gri
   int best_block = block0, best_grid = grid0;
   float best = -1.f;
   for (int block : {128, 256}) {
-    const int occ = mixed ? occupancy_f(c->prob0.tracking, c->all_iso, block) : occupancy_d(c->prob0.tracking, block);
+    const int occ = mixed ? occupancy_f(kernel_code(c), c->all_iso, block) : occupancy_d(kernel_code(c), block);
     for (int per_sm = 1; per_sm <= occ; per_sm++) {
       c->block = block;
       c->grid = c->nsm * per_sm;
@@ -1616,8 +1641,8 @@ static int transport_noalloc_impl(abx_ctx* c, unsigned char* scratch, const abx_
   A.st = c->st;
   A.trace = nullptr;
   A.max_events = c->max_events;
-  if constexpr (sizeof(R) == 4) launch_transport_f(A, c->prob0.tracking, c->all_iso, false, c->grid, c->block, c->stream);
-  else launch_transport_d(A, c->prob0.tracking, false, c->grid, c->block, c->stream);
+  if constexpr (sizeof(R) == 4) launch_transport_f(A, kernel_code(c), c->all_iso, false, c->grid, c->block, c->stream);
+  else launch_transport_d(A, kernel_code(c), false, c->grid, c->block, c->stream);
   CUDA_TRY(cudaGetLastError());
   unsigned nb = (unsigned)((n + SCAN_CHUNK - 1) / SCAN_CHUNK);
   if (nb == 0) nb = 1;
@@ -1641,8 +1666,8 @@ extern "C" int abx_transport_noalloc(abx_ctx* c, const abx_particle* bank_dev, s
                 NA_SITES, site_capacity);
   if (c->prob0.mode == ABX_MODE_FIXED_SOURCE && c->fissile_any)
     return fail(ABX_ERR_UNSUPPORTED, "fixed-source fission secondaries need abx_transport");
-  if (c->prob0.tracking == ABX_TRACK_CARTER)
-    return fail(ABX_ERR_UNSUPPORTED, "Carter tracking splits particles onto stacks: use abx_transport");
+  if (c->prob0.tracking == ABX_TRACK_CARTER || (c->prob0.branchless & ABX_BRANCHLESS_SPLITTING))
+    return fail(ABX_ERR_UNSUPPORTED, "splitting puts particles on stacks: use abx_transport");
   if (cudaSetDevice(c->device) != cudaSuccess) return fail(ABX_ERR_CUDA, "cudaSetDevice failed");
   unsigned char* scratch = nullptr;
   int rc = scratch_address(c->device, &scratch);

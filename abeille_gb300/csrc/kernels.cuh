@@ -51,7 +51,10 @@ template <class R> struct TransportArgs {
   unsigned long long* pcount;
 };
 
-enum : int { ABX_PSCORES = 5, ABX_PCOUNTS = 4 };  // counters: collisions flights histories lost
+enum : int { ABX_PSCORES = 5, ABX_PCOUNTS = 4 };
+// transport kernel codes: the tracking mode (ABX_TRACK_*) or'd with this bit
+// for branchless collisions
+enum : int { ABX_KERNEL_BRANCHLESS = 0x100 };  // counters: collisions flights histories lost
 
 template <class R> ABX_DEV View<R> make_view(const Tables& T);
 template <> ABX_DEV View<double> make_view<double>(const Tables& T) {
@@ -411,9 +414,137 @@ ABX_DEV FissionOut fission_dispatch(const TransportArgs<R>& A, const R* chi, con
 // Transporter::collision + branching_collision + russian_roulette +
 // make_fission_neutrons + do_scatter (src/transporter.cpp:35-93, 269-347, 358-487),
 // MGNuclide::sample_scatter / sample_fission (src/mg_nuclide.cpp:442-461, 504-544)
+// Particle::split (include/simulation/particle.hpp:165-173): n > 1 particles
+// of equal weight, the n - 1 copies on the history's secondary stack.
+template <class R> ABX_DEV void split_lane(const TransportArgs<R>& A, Lane<R>& L, int n) {
+  if (n <= 1) return;
+  L.w = L.w / (R)n;
+  L.w2 = L.w2 / (R)n;
+  const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int i = 0; i < n - 1; i++) {
+    if (L.nsec < A.sec_cap) {
+      R* sp = A.sec + ((uint64_t)gt * A.sec_cap + L.nsec) * 9;
+      sp[0] = L.r.x; sp[1] = L.r.y; sp[2] = L.r.z;
+      sp[3] = L.u.x; sp[4] = L.u.y; sp[5] = L.u.z;
+      sp[6] = L.E; sp[7] = L.w; sp[8] = L.w2;
+      L.nsec++;
+    } else {
+      raise_err(A.st, ABX_ERR_CAPACITY, L.h);
+      atomicAdd(&A.st->sec_overflow, 1ull);
+      return;
+    }
+  }
+}
+
+// Transporter::branchless_collision_iso / branchless_collision_mat
+// (src/transporter.cpp:95-267), after the collision scores: the collision
+// either scatters, its weight multiplied by m = (nu Sigma_f + Sigma_s) /
+// Sigma_t, or ends the history in one fission site of weight w m.  The
+// per-nuclide form draws the nuclide, scores k_abs, plays roulette, then
+// draws the reaction; the per-material form draws the reaction, then the
+// nuclide, scores k_abs scaled by m / m_i, then plays roulette.  A scattered
+// particle splits (floor(|w|) copies per nuclide, ceil(|w|) per material)
+// when splitting is on and |w| reaches wgt_split.
+template <class R, bool ISO>
+ABX_DEV void branchless_collide(const TransportArgs<R>& A, const Tables& T, const View<R>& V, const ProbT& P,
+                                const MatT& M, Lane<R>& L, Acc<R>& acc, bool& alive) {
+  const int G = M.G, g = L.g;
+  const R* xs = V.xs + M.xs_off;
+  const R Et = xs[XS_ET * G + g];
+  const R Eabs = xs[XS_EABS * G + g];
+  const R Ef = xs[XS_EF * G + g];
+  const R nu = xs[XS_NU * G + g];
+  const bool per_mat = (P.branchless & ABX_BRANCHLESS_MATERIAL) != 0;
+  bool scatter = false;
+  R m;
+  if (per_mat) {
+    const R Es = xs[XS_ES * G + g];
+    const R vEf = xs[XS_VEF * G + g];
+    const R Pscatter = Es / (vEf + Es);
+    m = (vEf + Es) / Et;
+    scatter = canon<R>(L.rng) < Pscatter;
+    (void)canon<R>(L.rng);  // sample_branchless_nuclide's draw (material_helper.hpp:226-271)
+    const R m_i = (nu * Ef + (Et - Eabs)) / Et;
+    acc.habs += (m / m_i) * L.w * nu * Ef / Et;
+  } else {
+    (void)canon<R>(L.rng);  // sample_nuclide's draw (material_helper.hpp:178-224)
+    acc.habs += L.w * nu * Ef / Et;
+  }
+  const R Pscatter_iso = (Et - Eabs) / (nu * Ef + (Et - Eabs));
+  if (!per_mat) m = (nu * Ef + (Et - Eabs)) / Et;
+  // russian roulette (src/transporter.cpp:35-58)
+  if (m_abs(L.w) < (R)P.wgt_cutoff) {
+    R P_kill = R(1) - (m_abs(L.w) / (R)P.wgt_survival);
+    if (canon<R>(L.rng) < P_kill) L.w = R(0);
+    else L.w = copysign((R)P.wgt_survival, L.w);
+  }
+  if (m_abs(L.w2) < (R)P.wgt_cutoff) {
+    R P_kill = R(1) - (m_abs(L.w2) / (R)P.wgt_survival);
+    if (canon<R>(L.rng) < P_kill) L.w2 = R(0);
+    else L.w2 = copysign((R)P.wgt_survival, L.w2);
+  }
+  const bool live = !(L.w == R(0) && L.w2 == R(0));
+  if (live && !per_mat) scatter = canon<R>(L.rng) < Pscatter_iso;
+  const bool fis = live && !scatter;
+  // one atomic per warp reserves the sites of every lane that ends in fission
+  uint64_t base = 0;
+  if (__any_sync(__activemask(), fis)) {
+    cg::coalesced_group grp = cg::coalesced_threads();
+    const unsigned my = fis ? 1u : 0u;
+    const unsigned pre = cg::exclusive_scan(grp, my);
+    const unsigned tot = cg::reduce(grp, my, cg::plus<unsigned>());
+    const double wsum = cg::reduce(grp, fis ? (double)(L.w * m) : 0., cg::plus<double>());
+    unsigned long long b0 = 0;
+    if (grp.thread_rank() == 0 && tot) {
+      b0 = atomicAdd(&A.st->site_count, (unsigned long long)tot);
+      atomicAdd(&A.st->site_wsum, wsum);
+    }
+    b0 = grp.shfl(b0, 0);
+    base = b0 + pre;
+  }
+  if (!live) {
+    alive = false;
+  } else if (scatter) {
+    int ei = discrete<R>(L.rng, V.cdf + M.cdf_off + g * G, G);
+    R E_out = group_mid(V, P, ei);
+    R mu = sample_mu<R, ISO>(T, V, M, g, ei, L.rng);
+    R c, s;
+    azimuth(canon<R>(L.rng), c, s);
+    L.u = rotate(L.u, mu, c, s);
+    L.E = E_out;
+    L.g = ei;
+    L.w = L.w * m * R(1);
+    L.w2 = L.w2 * m * R(1);
+    if ((double)L.E < P.min_energy) alive = false;
+    if ((P.branchless & ABX_BRANCHLESS_SPLITTING) && alive && m_abs(L.w) >= (R)P.wgt_split)
+      split_lane(A, L, per_mat ? (int)ceil((double)m_abs(L.w)) : (int)floor((double)m_abs(L.w)));
+  } else {
+    // MGNuclide::sample_fission (src/mg_nuclide.cpp:504-544), one neutron
+    const R P_delayed = xs[XS_NUD * G + g] / nu;
+    int ei = discrete<R>(L.rng, V.cdf + M.cdf_off + G * G + g * G, G);
+    R E_out = group_mid(V, P, ei);
+    R mu = R(2) * canon<R>(L.rng) - R(1);
+    R c, s;
+    azimuth(canon<R>(L.rng), c, s);
+    const V3<R> uo = rotate(L.u, mu, c, s);
+    if (canon<R>(L.rng) < P_delayed) (void)discrete<R>(L.rng, V.dgcdf + M.dg_off, M.ndg);
+    const R wsite = L.w * m;
+    if (base < A.site_cap) {
+      A.sites.x[base] = L.r.x; A.sites.y[base] = L.r.y; A.sites.z[base] = L.r.z;
+      A.sites.ux[base] = uo.x; A.sites.uy[base] = uo.y; A.sites.uz[base] = uo.z;
+      A.sites.E[base] = E_out; A.sites.w[base] = wsite;
+      A.sites.hist[base] = L.h; A.sites.dau[base] = L.dau;
+    }
+    L.dau++;
+    if (wsite > R(0)) L.npos++;
+    else L.nneg++;
+    alive = false;
+  }
+}
+
 // RESYNC reconverges the colliding lanes after the fission block (measured
-// faster with surface tracking only).
-template <class R, bool ISO, bool RESYNC>
+// faster with surface tracking only).  BL: branchless collisions.
+template <class R, bool ISO, bool RESYNC, bool BL>
 ABX_DEV void collide(const TransportArgs<R>& A, const Tables& T, const View<R>& V, const ProbT& P,
                      Lane<R>& L, Acc<R>& acc, bool converged, R kcol, bool& alive) {
   const unsigned cmask = RESYNC ? __activemask() : 0u;
@@ -433,6 +564,10 @@ ABX_DEV void collide(const TransportArgs<R>& A, const Tables& T, const View<R>& 
     R mig_scr = L.w * Eabs / Et * mig_dist * mig_dist;
     acc.hcol += k_col_scr;
     acc.hmig += mig_scr;
+  }
+  if constexpr (BL) {
+    branchless_collide<R, ISO>(A, T, V, P, M, L, acc, alive);
+    return;
   }
   (void)canon<R>(L.rng);  // sample_nuclide's draw (include/materials/material_helper.hpp:189)
   acc.habs += L.w * nu * Ef / Et;

@@ -41,13 +41,18 @@ void launch_sources_f(const SourceArgs& A, cudaStream_t s);  // transport_mixed.
 int transport_regs_d(int tracking);
 
 // transport_mixed.cu (+ transport_mixed_surface.cu); `iso`: every material
-// of the problem scatters isotropically
+// of the problem scatters isotropically; `tracking` is a kernel code (the
+// tracking mode, or'd with ABX_KERNEL_BRANCHLESS for branchless collisions)
 void launch_transport_f(const TransportArgs<float>& A, int tracking, bool iso, bool trace, int grid, int block,
                         cudaStream_t s);
 void launch_transport_f_surface(const TransportArgs<float>& A, bool iso, int grid, int block, cudaStream_t s);
 void launch_transport_f_variant(const TransportArgs<float>& A, int tracking, bool iso, int grid, int block,
                                 cudaStream_t s);
 int occupancy_f_variant(int tracking, bool iso, int block);
+// transport_mixed_branchless.cu: `tracking` delta or surface
+void launch_transport_f_branchless(const TransportArgs<float>& A, int tracking, bool iso, int grid, int block,
+                                   cudaStream_t s);
+int occupancy_f_branchless(int tracking, bool iso, int block);
 int transport_regs_f(int tracking);
 int transport_regs_f_surface();
 

@@ -89,7 +89,9 @@ struct ProbT {
   int32_t src_first, src_count;   // into the source pool
   int32_t src_cdf_off;            // discrete CDF over source weights
   float wgt_split_f;
-  double wgt_split;               // Carter tracking splits at |weight| >= this
+  double wgt_split;               // Carter tracking and branchless splitting split at |weight| >= this
+  int32_t branchless;             // ABX_BRANCHLESS_* flags (0: branching collisions)
+  int32_t pad2_;
 };
 
 struct Tables {
@@ -142,6 +144,7 @@ struct DevState {
   unsigned long long err_hist;
   unsigned long long trace_n;
   unsigned long long sec_overflow;
+  double site_wsum;               // sum of the fission sites' weights (branchless collisions)
 };
 
 }  // namespace abx

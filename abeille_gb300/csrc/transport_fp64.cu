@@ -12,10 +12,19 @@ template __global__ void transport_kernel<double, ABX_TRACK_SURFACE, false>(cons
 template __global__ void transport_kernel<double, ABX_TRACK_IMPLICIT_LEAKAGE, false>(
     const __grid_constant__ TransportArgs<double>);
 template __global__ void transport_kernel<double, ABX_TRACK_CARTER, false>(const __grid_constant__ TransportArgs<double>);
+// branchless collisions (the branchless k-eigenvalue simulation)
+template __global__ void transport_kernel<double, ABX_TRACK_DELTA | ABX_KERNEL_BRANCHLESS, false>(
+    const __grid_constant__ TransportArgs<double>);
+template __global__ void transport_kernel<double, ABX_TRACK_SURFACE | ABX_KERNEL_BRANCHLESS, false>(
+    const __grid_constant__ TransportArgs<double>);
 
 void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace, int grid, int block,
                         cudaStream_t s) {
-  if (tracking == ABX_TRACK_DELTA) {
+  if (tracking == (ABX_TRACK_DELTA | ABX_KERNEL_BRANCHLESS)) {
+    transport_kernel<double, ABX_TRACK_DELTA | ABX_KERNEL_BRANCHLESS, false><<<grid, block, 0, s>>>(A);
+  } else if (tracking == (ABX_TRACK_SURFACE | ABX_KERNEL_BRANCHLESS)) {
+    transport_kernel<double, ABX_TRACK_SURFACE | ABX_KERNEL_BRANCHLESS, false><<<grid, block, 0, s>>>(A);
+  } else if (tracking == ABX_TRACK_DELTA) {
     transport_kernel<double, ABX_TRACK_DELTA, false><<<grid, block, 0, s>>>(A);
   } else if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE) {
     transport_kernel<double, ABX_TRACK_IMPLICIT_LEAKAGE, false><<<grid, block, 0, s>>>(A);
@@ -28,7 +37,13 @@ void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace
 
 int occupancy_d(int tracking, int block) {
   int nb = 0;
-  if (tracking == ABX_TRACK_DELTA)
+  if (tracking == (ABX_TRACK_DELTA | ABX_KERNEL_BRANCHLESS))
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &nb, transport_kernel<double, ABX_TRACK_DELTA | ABX_KERNEL_BRANCHLESS, false>, block, 0);
+  else if (tracking == (ABX_TRACK_SURFACE | ABX_KERNEL_BRANCHLESS))
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &nb, transport_kernel<double, ABX_TRACK_SURFACE | ABX_KERNEL_BRANCHLESS, false>, block, 0);
+  else if (tracking == ABX_TRACK_DELTA)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_DELTA, false>, block, 0);
   else if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<double, ABX_TRACK_IMPLICIT_LEAKAGE, false>,

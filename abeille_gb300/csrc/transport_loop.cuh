@@ -144,9 +144,13 @@ ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& ac
 // Occupancy (measured on config 1 and config 2): FP32 delta tracking (and
 // implicit-leakage delta tracking) runs four 256-thread blocks per SM (64
 // registers), FP32 surface tracking three (80 registers), FP64 three (80).
+// TRACK: the tracking mode, or'd with ABX_KERNEL_BRANCHLESS for the
+// branchless collisions of the branchless k-eigenvalue simulation.
 template <class R, int TRACK, bool ISO>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURFACE ? 4 : 3) : 3)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_TRACK_SURFACE ? 4 : 3) : 3)
     transport_kernel(const __grid_constant__ TransportArgs<R> A) {
+  constexpr int TRK = TRACK & 0xff;
+  constexpr bool BL = (TRACK & ABX_KERNEL_BRANCHLESS) != 0;
   const bool TRACE = A.trace != nullptr;
   const Tables& T = A.T;
   const View<R> V = make_view<R>(T);
@@ -224,7 +228,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
       const ProbT& P = T.probs[L.pid];
       L.events++;
       nflight++;
-      if (TRACK == ABX_TRACK_IMPLICIT_LEAKAGE) {
+      if (TRK == ABX_TRACK_IMPLICIT_LEAKAGE) {
         // ImplicitLeakageDeltaTracker::transport
         // (src/implicit_leakage_delta_tracker.cpp:104-214): the nearest
         // boundary condition before every flight; towards a vacuum boundary
@@ -282,11 +286,11 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
             ph = PH_MOVED;
           }
         }
-      } else if (TRACK == ABX_TRACK_DELTA || TRACK == ABX_TRACK_CARTER) {
+      } else if (TRK == ABX_TRACK_DELTA || TRK == ABX_TRACK_CARTER) {
         // DeltaTracker::transport (src/delta_tracker.cpp:105-118); Carter
         // tracking flies the same way on its sampling cross section
         // (src/carter_tracker.cpp:124-138), stored after the majorant
-        const R Emaj = V.maj[P.maj_off + (TRACK == ABX_TRACK_CARTER ? P.G : 0) + L.g];
+        const R Emaj = V.maj[P.maj_off + (TRK == ABX_TRACK_CARTER ? P.G : 0) + L.g];
         dcol = Emaj == R(0) ? Tol<R>::INF : -m_log(R(1) - canon<R>(L.rng)) / Emaj;
         trk_move(k, dcol);
         const int r = trk_check(T, V, k, dui, dfr);
@@ -380,7 +384,14 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
         ph = PH_FLIGHT;
       }
     } else if (ph == PH_RES) {
-      if (k.cell < 0) ABX_FAIL(ABX_ERR_LOST_PARTICLE) else {
+      if (k.cell < 0) {
+        // a secondary starting on a boundary that FP32 rounding puts outside:
+        // counted in `lost` and killed in the mixed mode, fatal in FP64
+        if (sizeof(R) == 8) ABX_FAIL(ABX_ERR_LOST_PARTICLE) else {
+          ABX_LOST();
+          ph = PH_DEAD;
+        }
+      } else {
         L.mat = T.cells[k.cell].fill;
         if (TRACE) trace_rec(A, L, 6, k.cell);
         ph = PH_FLIGHT;
@@ -419,7 +430,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
     // ----------------------------------------------------------------- moved
     __syncwarp();
     if (ph == PH_MOVED) {
-      if (k.cell < 0 && (TRACK == ABX_TRACK_DELTA || TRACK == ABX_TRACK_CARTER)) {
+      if (k.cell < 0 && (TRK == ABX_TRACK_DELTA || TRK == ABX_TRACK_CARTER)) {
         // flew out of the geometry: back to the last position, find the
         // boundary condition (src/delta_tracker.cpp:120-127)
         trk_set_r(k, L.r);
@@ -434,12 +445,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
         }
       } else {
         const ProbT& P = T.probs[L.pid];
-        if (TRACK != ABX_TRACK_IMPLICIT_LEAKAGE && converged && P.has_tle) score_flight(T, V, P, L, dcol);
+        if (TRK != ABX_TRACK_IMPLICIT_LEAKAGE && converged && P.has_tle) score_flight(T, V, P, L, dcol);
         L.r = add(L.r, scl(L.u, dcol));
         L.mat = T.cells[k.cell].fill;
         const MatT& M = T.mats[L.mat];
         const R Et = V.xs[M.xs_off + XS_ET * M.G + L.g];
-        if (TRACK == ABX_TRACK_CARTER) {
+        if (TRK == ABX_TRACK_CARTER) {
           // src/carter_tracker.cpp:184-207: where the sampling cross section
           // falls below the total one the collision is always "real" with
           // probability D and carries weight factors +-F
@@ -502,7 +513,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
       bool alive = true;
       ncoll++;
       L.hcoll++;
-      collide<R, ISO, TRACK == ABX_TRACK_SURFACE>(A, T, V, P, L, acc, converged, kcol, alive);
+      collide<R, ISO, TRK == ABX_TRACK_SURFACE, BL>(A, T, V, P, L, acc, converged, kcol, alive);
       if (sizeof(R) == 4 && !(m_abs(L.u.x) <= R(1) && m_abs(L.u.y) <= R(1) && m_abs(L.u.z) <= R(1))) {
         // mixed mode: a direction that is not finite cannot be tracked
         ABX_LOST();
@@ -510,7 +521,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (TRACK != ABX_TRACK_SURF
       }
       k.u = L.u;
       if (TRACE) trace_rec(A, L, 4, k.cell);
-      if (TRACK == ABX_TRACK_CARTER && alive) carter_split(A, P, L);
+      if (TRK == ABX_TRACK_CARTER && alive) carter_split(A, P, L);
       ph = alive ? PH_FLIGHT : PH_DEAD;
     }
 

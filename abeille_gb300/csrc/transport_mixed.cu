@@ -14,7 +14,9 @@ template __global__ void transport_kernel<float, ABX_TRACK_DELTA, true>(const __
 
 void launch_transport_f(const TransportArgs<float>& A, int tracking, bool iso, bool trace, int grid, int block,
                         cudaStream_t s) {
-  if (tracking == ABX_TRACK_SURFACE) {
+  if (tracking & ABX_KERNEL_BRANCHLESS) {
+    launch_transport_f_branchless(A, tracking & 0xff, iso, grid, block, s);
+  } else if (tracking == ABX_TRACK_SURFACE) {
     launch_transport_f_surface(A, iso, grid, block, s);
   } else if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE || tracking == ABX_TRACK_CARTER) {
     launch_transport_f_variant(A, tracking, iso, grid, block, s);
@@ -26,6 +28,7 @@ void launch_transport_f(const TransportArgs<float>& A, int tracking, bool iso, b
 }
 
 int occupancy_f(int tracking, bool iso, int block) {
+  if (tracking & ABX_KERNEL_BRANCHLESS) return occupancy_f_branchless(tracking & 0xff, iso, block);
   if (tracking == ABX_TRACK_SURFACE) return occupancy_f_surface(iso, block);
   if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE || tracking == ABX_TRACK_CARTER)
     return occupancy_f_variant(tracking, iso, block);

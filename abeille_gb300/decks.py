@@ -274,12 +274,19 @@ def from_reference_deck(deck, nparticles=None, precision="fp64", tracking=None):
     st = deck["settings"]
     G = int(st["ngroups"])
     b = ProblemBuilder(G, [float(e) for e in st["energy-bounds"]],
-                       mode={"k-eigenvalue": "k-eigenvalue", "fixed-source": "fixed-source"}[st["simulation"]],
+                       mode={"k-eigenvalue": "k-eigenvalue", "fixed-source": "fixed-source",
+                             "branchless-k-eigenvalue": "branchless-k-eigenvalue"}[st["simulation"]],
                        tracking=tracking or st.get("transport", "surface-tracking"), precision=precision,
                        nparticles=nparticles or int(st["nparticles"]),
                        seed=int(st.get("seed", 19073486328125)), stride=int(st.get("stride", 152917)),
                        wgt_cutoff=float(st.get("wgt-cutoff", 0.25)), wgt_survival=float(st.get("wgt-survival", 1.0)),
-                       wgt_split=float(st.get("wgt-split", 2.0)), sampling_xs_ratio=deck.get("sampling-xs-ratio"))
+                       wgt_split=float(st.get("wgt-split", 2.0)), sampling_xs_ratio=deck.get("sampling-xs-ratio"),
+                       branchless_material=bool(st.get("branchless-material", True)),
+                       branchless_splitting=bool(st.get("branchless-splitting", False)))
+    if st["simulation"] == "branchless-k-eigenvalue" and st.get("branchless-combing", True):
+        # BranchlessPowerIterator::comb_particles (src/branchless_power_iterator.cpp:592-650),
+        # the reference's default, shuffles the bank with the global stream
+        raise ValueError("branchless-combing is not supported: set branchless-combing: false")
     for m in deck["materials"]:
         leg = {l: m[f"P{l}"] for l in range(1, 6) if f"P{l}" in m}
         b.material(int(m["id"]), total=m["total"], absorption=m["absorption"], scatter=m["scatter"],

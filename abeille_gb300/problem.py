@@ -98,7 +98,8 @@ def _ptr(arr, ctype):
 class ProblemBuilder:
     def __init__(self, ngroups, energy_bounds, mode="k-eigenvalue", tracking="delta-tracking",
                  precision="fp64", nparticles=10000, seed=19073486328125, stride=152917,
-                 wgt_cutoff=0.25, wgt_survival=1.0, block_size=0, wgt_split=2.0, sampling_xs_ratio=None):
+                 wgt_cutoff=0.25, wgt_survival=1.0, block_size=0, wgt_split=2.0, sampling_xs_ratio=None,
+                 branchless_material=True, branchless_splitting=False):
         self.G = int(ngroups)
         self.energy_bounds = np.asarray(energy_bounds, dtype=np.float64)
         if self.energy_bounds.shape != (self.G + 1,):
@@ -107,6 +108,10 @@ class ProblemBuilder:
         self.nparticles, self.seed, self.stride = nparticles, seed, stride
         self.wgt_cutoff, self.wgt_survival, self.block_size = wgt_cutoff, wgt_survival, block_size
         self.wgt_split = wgt_split
+        # mode "branchless-k-eigenvalue": the branchless collisions of
+        # BranchlessPowerIterator (settings branchless-material / -splitting,
+        # defaults as src/settings.cpp:87-89)
+        self.branchless_material, self.branchless_splitting = bool(branchless_material), bool(branchless_splitting)
         self.sampling_xs_ratio = None if sampling_xs_ratio is None else [float(x) for x in sampling_xs_ratio]
         self.surfaces, self.cells, self.universes, self.materials = [], [], {}, []
         self.universe_decl = []
@@ -291,6 +296,9 @@ class ProblemBuilder:
         settings = {"nparticles": int(self.nparticles), "ngroups": G, "transport": self.tracking,
                     "simulation": self.mode, "energy-mode": "multi-group",
                     "energy-bounds": self.energy_bounds.tolist(), "seed": int(self.seed), "stride": int(self.stride)}
+        if self.mode == "branchless-k-eigenvalue":
+            settings["branchless-material"] = self.branchless_material
+            settings["branchless-splitting"] = self.branchless_splitting
         if ngenerations is not None:
             settings["ngenerations"] = int(ngenerations)
         if nignored is not None:
@@ -429,6 +437,10 @@ class ProblemBuilder:
         s.nparticles = float(self.nparticles)
         s.block_size = self.block_size
         s.wgt_split = self.wgt_split
+        s.branchless = 0
+        if self.mode == "branchless-k-eigenvalue":
+            s.branchless = (abi.BRANCHLESS_ON | (abi.BRANCHLESS_MATERIAL if self.branchless_material else 0) |
+                            (abi.BRANCHLESS_SPLITTING if self.branchless_splitting else 0))
         p.energy_bounds = _ptr(eb, C.c_double)
         p.surfaces = C.cast(surf, C.POINTER(abi.Surface))
         p.n_surfaces = len(self.surfaces)

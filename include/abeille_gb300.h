@@ -204,7 +204,26 @@ typedef struct abx_settings {
   int32_t reserved;
   double wgt_split;   /* 2.0 (src/settings.cpp:64): Carter tracking splits a
                          particle whose |weight| reaches it                  */
+  int32_t branchless; /* ABX_BRANCHLESS_* flags; non-zero with
+                         ABX_MODE_K_EIGENVALUE = the reference's
+                         branchless-k-eigenvalue simulation               */
+  int32_t reserved2;
 } abx_settings;
+
+/* Branchless collisions (Transporter::branchless_collision,
+ * src/transporter.cpp:95-267), the collisions of the reference's
+ * branchless-k-eigenvalue simulation (BranchlessPowerIterator; its power
+ * iteration normalises the fission bank's weights as the k-eigenvalue one
+ * does).  Each collision either scatters with its weight multiplied by
+ * (nu Sigma_f + Sigma_s) / Sigma_t or ends the history in one fission site of
+ * that weight.  ON selects the per-nuclide form (branchless_collision_iso),
+ * ON | MATERIAL the per-material one (settings branchless-material),
+ * SPLITTING splits particles whose |weight| reaches wgt_split (settings
+ * branchless-splitting).  The reference's bank combing and regional
+ * cancellation are not part of this path (the deck reader refuses
+ * branchless-combing).  Delta and surface tracking only; abx_create returns
+ * ABX_ERR_UNSUPPORTED for other combinations. */
+enum { ABX_BRANCHLESS_ON = 1, ABX_BRANCHLESS_MATERIAL = 2, ABX_BRANCHLESS_SPLITTING = 4 };
 
 /* ------------------------------------------------------------- problem */
 typedef struct abx_problem {

@@ -1015,6 +1015,85 @@ static void russian_roulette(oracle_ctx* ctx, Part* p) {
   if (p->s.w == 0. && p->s.w2 == 0.) p->alive = 0;
 }
 
+/* Transporter::branchless_collision_iso / branchless_collision_mat
+ * (src/transporter.cpp:95-267), after Transporter::collision's scores: the
+ * collision scatters with the weight multiplied by m, or ends the history in
+ * one fission site of weight w m.  Splitting: Particle::split
+ * (include/simulation/particle.hpp:165-173). */
+static int branchless_collision(oracle_ctx* ctx, Part* p, int mat, int g, Scores* sc, SiteBuf* sb, uint32_t h) {
+  const int G = ctx->G;
+  const double Et = MAT_AT(ctx->Et, mat, g);
+  const double Eabs = MAT_AT(ctx->Eabs, mat, g);
+  const double Ef = MAT_AT(ctx->Ef, mat, g);
+  const double nu = MAT_AT(ctx->nu_tot, mat, g);
+  const int per_mat = (ctx->set.branchless & ABX_BRANCHLESS_MATERIAL) != 0;
+  const int splitting = (ctx->set.branchless & ABX_BRANCHLESS_SPLITTING) != 0;
+  const double wgt_split = ctx->set.wgt_split > 0. ? ctx->set.wgt_split : 2.0;
+  int scatter;
+  double m;
+  if (per_mat) {
+    /* branchless_collision_mat (src/transporter.cpp:185-267) */
+    const double Es = MAT_AT(ctx->Es, mat, g);
+    const double vEf = MAT_AT(ctx->vEf, mat, g);
+    const double Pscatter = Es / (vEf + Es);
+    m = (vEf + Es) / Et;
+    scatter = oracle_canonical(&p->rng) < Pscatter;
+    (void)oracle_canonical(&p->rng); /* sample_branchless_nuclide (material_helper.hpp:226-271) */
+    const double m_i = (nu * Ef + (Et - Eabs)) / Et;
+    sc->k_abs += (m / m_i) * p->s.w * nu * Ef / Et;
+    russian_roulette(ctx, p);
+    if (!p->alive) return ABX_OK;
+  } else {
+    /* branchless_collision_iso (src/transporter.cpp:104-183) */
+    (void)oracle_canonical(&p->rng); /* sample_nuclide */
+    sc->k_abs += p->s.w * nu * Ef / Et;
+    const double Pscatter = (Et - Eabs) / (nu * Ef + (Et - Eabs));
+    m = (nu * Ef + (Et - Eabs)) / Et;
+    russian_roulette(ctx, p);
+    if (!p->alive) return ABX_OK;
+    scatter = oracle_canonical(&p->rng) < Pscatter;
+  }
+  if (scatter) {
+    int ei = sample_discrete_cdf(&p->rng, ctx->ps_cdf + ((size_t)mat * G + g) * G, G);
+    double E_out = group_mid(ctx, ei);
+    double mu = sample_mu(ctx, mat, g, ei, &p->rng);
+    double phi = 2. * PI_ * oracle_canonical(&p->rng);
+    p->s.E = E_out;
+    p->s.u = rotate_direction(p->s.u, mu, phi);
+    p->s.w = p->s.w * m * 1.;
+    p->s.w2 = p->s.w2 * m * 1.;
+    if (p->s.E < ctx->min_energy) p->alive = 0;
+    if (splitting && p->alive && fabs(p->s.w) >= wgt_split) {
+      int n_new = per_mat ? (int)ceil(fabs(p->s.w)) : (int)floor(fabs(p->s.w));
+      if (n_new > 1) {
+        p->s.w = p->s.w / (double)n_new;
+        p->s.w2 = p->s.w2 / (double)n_new;
+        for (int k = 0; k < n_new - 1; k++)
+          if (!sec_push(p, p->s)) { set_err("out of memory"); return ABX_ERR_OOM; }
+      }
+    }
+  } else {
+    /* MGNuclide::sample_fission (src/mg_nuclide.cpp:504-544), one neutron */
+    double P_delayed = MAT_AT(ctx->nu_d, mat, g) / nu;
+    int ei = sample_discrete_cdf(&p->rng, ctx->chi_cdf + ((size_t)mat * G + g) * G, G);
+    double E_out = group_mid(ctx, ei);
+    double mu = 2. * oracle_canonical(&p->rng) - 1.;
+    double phi = 2. * PI_ * oracle_canonical(&p->rng);
+    V3 uout = rotate_direction(p->s.u, mu, phi);
+    if (oracle_canonical(&p->rng) < P_delayed) (void)sample_discrete_cdf(&p->rng, ctx->dg_cdf[mat], ctx->n_dg[mat]);
+    abx_site s;
+    s.r[0] = p->s.r.x; s.r[1] = p->s.r.y; s.r[2] = p->s.r.z;
+    s.u[0] = uout.x; s.u[1] = uout.y; s.u[2] = uout.z;
+    s.E = E_out; s.wgt = p->s.w * m; s.wgt2 = 0.; /* the next generation starts from wgt alone */
+    s.parent_history_id = p->hid;
+    s.parent_daughter_id = p->daughter++;
+    s.family_id = p->family;
+    if (!site_push(sb, h, &s)) { set_err("out of memory"); return ABX_ERR_OOM; }
+    p->alive = 0;
+  }
+  return ABX_OK;
+}
+
 /* Transporter::collision + branching_collision + make_fission_neutrons +
  * do_scatter (src/transporter.cpp:60-93, 269-347, 358-487) and
  * MGNuclide::sample_scatter / sample_fission (src/mg_nuclide.cpp:442-461, 504-544) */
@@ -1035,6 +1114,7 @@ static int collision(oracle_ctx* ctx, Part* p, int mat, double kcol, int converg
     sc->k_col += k_col_scr;
     sc->mig += mig_area_scr;
   }
+  if (ctx->set.branchless) return branchless_collision(ctx, p, mat, g, sc, sb, h);
   /* sample_nuclide: one draw even with a single component (material_helper.hpp:178-224) */
   (void)oracle_canonical(&p->rng);
   double k_abs_scr = p->s.w * nu * Ef / Et;

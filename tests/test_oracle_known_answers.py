@@ -67,6 +67,31 @@ def test_carter_tracking_signed_weights_fixed_source():
     assert abs(l1 - l2) < 4 * np.hypot(s1, s2), res
 
 
+@pytest.mark.parametrize("name,material,splitting,tracking", [
+    ("PUa-1-0-IN", True, False, "delta-tracking"), ("PUb-1-0-IN", False, False, "delta-tracking"),
+    ("PUa-1-0-SL", True, True, "surface-tracking"), ("PUb-1-0-SL", False, True, "delta-tracking")])
+def test_branchless_collisions_analytic_k(name, material, splitting, tracking):
+    """The branchless k-eigenvalue simulation (branchless collisions: scatter
+    with the weight multiplied by (nu Sigma_f + Sigma_s) / Sigma_t, or one
+    fission site; per material or per nuclide; with and without splitting;
+    bank weights normalised to N, no combing): the analytic k."""
+    deck = json.loads(json.dumps(DECKS[name]))
+    st_ = deck["settings"]
+    st_.update({"simulation": "branchless-k-eigenvalue", "branchless-combing": False,
+                "branchless-material": material, "branchless-splitting": splitting})
+    b = decks.from_reference_deck(deck, nparticles=20000, tracking=tracking)
+    st, _, _ = oracle.Oracle(b.build(), nthreads=oracle.cores()).run_power_iteration(50, 10)
+    assert st["kcol_std"] > 0
+    assert abs(st["kcol_avg"] - DECKS[name]["_expected_k"]) < 4 * st["kcol_std"] + 1e-4, st
+
+
+def test_branchless_combing_is_refused():
+    deck = json.loads(json.dumps(DECKS["PUa-1-0-IN"]))
+    deck["settings"]["simulation"] = "branchless-k-eigenvalue"
+    with pytest.raises(ValueError):
+        decks.from_reference_deck(deck, nparticles=1000)
+
+
 @pytest.mark.parametrize("name", ["Ua-1-1-CY", "UD2O-2-1-SL"])
 def test_delta_and_surface_tracking_agree(name):
     deck = DECKS[name]
