@@ -33,7 +33,7 @@ def run_deck(path_or_text, precision="mixed", particles=None, generations=None, 
     nign = int(ignored if ignored is not None else st.get("nignored", 0 if builder.mode == "fixed-source" else 10))
     eng = Engine(builder.build(precision=precision), device)
     try:
-        if builder.mode == "k-eigenvalue":
+        if builder.mode != "fixed-source":  # k-eigenvalue, branching or branchless
             stats, recs = eng.run_power_iteration_records(ngen, nign)
             print(f" {'gen':>5} {'k_col':>10} {'entropy':>10}", file=out)
             for i, r in enumerate(recs):
