@@ -1809,6 +1809,7 @@ extern "C" int abx_entropy(abx_ctx* c, const abx_site* s, size_t n, double* H) {
 
 extern "C" int abx_set_trace(abx_ctx* c, uint32_t n_hist, size_t cap) {
   if (!c) return fail(ABX_ERR_INVALID, "null context");
+  if (mixed_of(c) && n_hist && cap) return fail(ABX_ERR_UNSUPPORTED, "event traces are recorded in the FP64 mode");
   cudaSetDevice(c->device);
   if (c->trace) cudaFree(c->trace);
   c->trace = nullptr;

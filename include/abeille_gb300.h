@@ -511,11 +511,13 @@ int abx_server_get_stats(abx_server* server, abx_server_stats* stats);
 /* Per-event trace of the first `n_hist` histories of the next abx_transport
  * call (test hook).  Each record: history index, event kind, rng state,
  * position, direction, group, weight.  Records go to `out` (capacity in
- * records); *n_out receives the count.  Pass n_hist = 0 to disable. */
+ * records); *n_out receives the count.  Pass n_hist = 0 to disable.  FP64
+ * mode only (ABX_ERR_UNSUPPORTED on a mixed-precision context: the FP32
+ * kernels carry no trace code). */
 typedef struct abx_trace_rec {
   uint32_t hist;
   int32_t kind;  /* 0 flight-virtual 1 flight-real 2 leak 3 reflect 4 collision-done 5 cross
-                    6 resurrect 7 lost (mixed mode: counted and ended)              */
+                    6 resurrect 7 lost                                               */
   int32_t group;
   int32_t cell;
   uint64_t rng_state;
