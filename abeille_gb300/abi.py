@@ -203,6 +203,7 @@ PROTOTYPES = {
     "abx_tally_read_all": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "abx_read_source_bank": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t),
                                        C.POINTER(C.c_double)]),
+    "abx_set_source_bank": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "abx_server_create": (C.c_int, [C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
     "abx_server_destroy": (C.c_int, [C.c_void_p]),
     "abx_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.c_uint64, C.POINTER(C.c_uint64)]),

@@ -753,6 +753,9 @@ struct abx_context {
   int pi_bank = -1;
   size_t pi_n = 0;
   double pi_kcol = 1.;
+  // a source bank to start the next power iteration from (x y z ux uy uz E
+  // w w2 per particle), set by abx_set_source_bank; empty: sample the sources
+  std::vector<double> restart_src;
   cudaGraphExec_t gen_exec[2] = {nullptr, nullptr};
   cudaGraph_t gen_graph[2] = {nullptr, nullptr};  // kept: exec updates name its nodes
   cudaGraphNode_t gen_ev_node[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -1956,6 +1959,63 @@ extern "C" int abx_set_graphs(abx_ctx* c, int enabled) {
   return ABX_OK;
 }
 
+// PowerIterator::load_source_from_file (src/power_iterator.cpp:60-132): the
+// stored particles become histories 0..n-1 (family = history id), each
+// stream seeded at its id.  The caller has already set nparticles to the
+// rounded total weight on the host; it is copied to the device here (and
+// stays so for the context).
+static int load_restart_bank(abx_ctx* c, bool mixed, size_t cap, size_t* n_out) {
+  const size_t n = c->restart_src.size() / 9;
+  if (n > cap) return fail(ABX_ERR_CAPACITY, "source bank of %zu particles, capacity %zu", n, cap);
+  std::vector<abx_particle> bank(n);
+  for (size_t i = 0; i < n; i++) {
+    const double* q = c->restart_src.data() + 9 * i;
+    abx_particle& p = bank[i];
+    for (int a = 0; a < 3; a++) { p.r[a] = q[a]; p.u[a] = q[3 + a]; }
+    p.E = q[6];
+    p.wgt = q[7];
+    p.wgt2 = q[8];
+    p.history_id = i;
+    p.family_id = i;
+    p.rng_state = pcg_advance(pcg_seeded(c->prob0.seed), c->prob0.stride * (uint64_t)i);
+  }
+  // the run's nparticles (set from the bank's total weight) on the device
+  CUDA_TRY(cudaMemcpyAsync((void*)c->D.T.probs, &c->P.probs[0], sizeof(ProbT), cudaMemcpyHostToDevice, c->stream));
+  if (c->aos_in_cap < n) {
+    if (c->aos_in) cudaFree(c->aos_in);
+    c->aos_in = nullptr;
+    c->aos_in_cap = 0;
+    CUDA_TRY(cudaMalloc(&c->aos_in, n * sizeof(abx_particle)));
+    c->aos_in_cap = n;
+  }
+  CUDA_TRY(cudaMemcpyAsync(c->aos_in, bank.data(), n * sizeof(abx_particle), cudaMemcpyHostToDevice, c->stream));
+  if (mixed) k_bank_from_aos<float><<<grid_for(n), 256, 0, c->stream>>>(c->aos_in, n, c->bf[0].b);
+  else k_bank_from_aos<double><<<grid_for(n), 256, 0, c->stream>>>(c->aos_in, n, c->bd[0].b);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(c->stream));  // `bank` is pageable host memory
+  *n_out = n;
+  return ABX_OK;
+}
+
+extern "C" int abx_set_source_bank(abx_ctx* c, const double* source, size_t n) {
+  if (!c || (!source && n)) return fail(ABX_ERR_INVALID, "bad arguments");
+  if (c->prob0.mode != ABX_MODE_K_EIGENVALUE) return fail(ABX_ERR_INVALID, "problem is not k-eigenvalue");
+  if (n == 0) {
+    c->restart_src.clear();
+    return ABX_OK;
+  }
+  const double* eb = c->P.eb_d.data() + c->prob0.eb_off;
+  for (size_t i = 0; i < n; i++) {
+    const double* q = source + 9 * i;
+    for (int a = 0; a < 9; a++)
+      if (!std::isfinite(q[a])) return fail(ABX_ERR_INVALID, "source particle %zu: value %d is not finite", i, a);
+    if (!(q[6] >= eb[0] && q[6] <= eb[c->prob0.G]))
+      return fail(ABX_ERR_INVALID, "source particle %zu: energy outside the group structure", i);
+  }
+  c->restart_src.assign(source, source + 9 * n);
+  return ABX_OK;
+}
+
 extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, abx_run_stats* stats,
                                           abx_gen_record* per_gen) {
   if (!c || ngen <= 0 || nignored < 0) return fail(ABX_ERR_INVALID, "bad arguments");
@@ -1963,8 +2023,21 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
   cudaSetDevice(c->device);
   const bool mixed = mixed_of(c);
   int rc;
+  const size_t n_restart = c->restart_src.size() / 9;
+  if (n_restart) {
+    // settings::nparticles and the tallies' total weight become the source
+    // bank's rounded total weight (src/power_iterator.cpp:124-131)
+    double tot_wgt = 0.;
+    for (size_t i = 0; i < n_restart; i++) tot_wgt += c->restart_src[9 * i + 7];
+    const double np = std::round(tot_wgt);
+    if (!(np > 0.)) return fail(ABX_ERR_INVALID, "source bank has no positive total weight");
+    for (ProbT* q : {&c->prob0, &c->P.probs[0]}) {
+      q->nparticles = np;
+      q->inv_np = 1. / np;
+    }
+  }
   const size_t N = (size_t)c->prob0.nparticles;
-  const size_t cap = 3 * N + 4096;
+  const size_t cap = 3 * std::max(N, n_restart) + 4096;
   if ((rc = ensure_banks(c, cap, mixed, false)) != ABX_OK) return rc;
   if ((rc = ensure_sites(c, cap, mixed)) != ABX_OK) return rc;
   if ((rc = ensure_records(c, ngen)) != ABX_OK) return rc;
@@ -1975,21 +2048,26 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
   zero_d(c->tally_avg, (size_t)c->P.tally_bins, c->stream);
   zero_d(c->tally_var, (size_t)c->P.tally_bins, c->stream);
   c->tally_g = 0;
-  // initial source bank, histories 0..N-1 (src/power_iterator.cpp:135-166)
-  SourceArgs S{};
-  S.T = c->D.T;
-  S.prob = 0;
-  S.first_hid = 0;
-  S.n = N;
-  sample_bank0(c, S, mixed, false);
+  size_t N0 = N;  // histories of the first generation
+  if (c->restart_src.empty()) {
+    // initial source bank, histories 0..N-1 (src/power_iterator.cpp:135-166)
+    SourceArgs S{};
+    S.T = c->D.T;
+    S.prob = 0;
+    S.first_hid = 0;
+    S.n = N;
+    sample_bank0(c, S, mixed, false);
+  } else if ((rc = load_restart_bank(c, mixed, cap, &N0)) != ABX_OK) {
+    return rc;
+  }
   {
-    // RunAcc.global_hist = N; DevState: n_hist = N, kcol = 1, converged
+    // RunAcc.global_hist = N0; DevState: n_hist = N0, kcol = 1, converged
     RunAcc ra{};
-    ra.global_hist = N;
+    ra.global_hist = N0;
     CUDA_TRY(cudaMemcpyAsync(c->run, &ra, sizeof ra, cudaMemcpyHostToDevice, c->stream));
   }
   if ((rc = check_state(c)) != ABX_OK) return rc;
-  k_step_begin<<<1, 1, 0, c->stream>>>(c->st, N, 1.0, nignored == 0 ? 1 : 0, 0);
+  k_step_begin<<<1, 1, 0, c->stream>>>(c->st, N0, 1.0, nignored == 0 ? 1 : 0, 0);
   if ((rc = ensure_sec(c, mixed)) != ABX_OK) return rc;
   // the generation events come from the context's pool and live as long as
   // the context: a captured graph's event nodes keep pointing at them

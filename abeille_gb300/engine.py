@@ -97,6 +97,21 @@ class Engine:
         self._chk(self.lib.abx_read_source_bank(self.ctx, bank.ctypes.data, n.value, C.byref(n), C.byref(k)))
         return bank, k.value
 
+    def set_source_bank(self, source):
+        """Start the next power iterations from a stored source bank: rows
+        x y z ux uy uz E wgt wgt2 (the reference's source file layout);
+        None or an empty array goes back to sampling the sources."""
+        if source is None or len(source) == 0:
+            self._chk(self.lib.abx_set_source_bank(self.ctx, None, 0))
+            return
+        src = np.ascontiguousarray(source, dtype=np.float64).reshape(-1, 9)
+        self._chk(self.lib.abx_set_source_bank(self.ctx, src.ctypes.data, src.shape[0]))
+
+    @staticmethod
+    def source_rows(bank):
+        """Particles (PARTICLE_DTYPE) as source-file rows x y z ux uy uz E wgt wgt2."""
+        return np.column_stack([bank["r"], bank["u"], bank["E"], bank["wgt"], bank["wgt2"]])
+
     def tally_all(self):
         """Average and variance of every tally bin of the context (in a batch
         context: every problem's bins, problem after problem), in one read."""

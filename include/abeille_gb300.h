@@ -395,6 +395,19 @@ int abx_run_power_iteration_ex(abx_ctx* ctx, int ngenerations, int nignored,
 int abx_read_source_bank(abx_ctx* ctx, abx_particle* out, size_t capacity,
                          size_t* n_out, double* kcol_out);
 
+/* Start the next abx_run_power_iteration[_ex] of the context from a stored
+ * source bank instead of the problem's sources: the reference's source-file
+ * restart (PowerIterator::load_source_from_file,
+ * src/power_iterator.cpp:60-132).  `source` holds n rows of 9 doubles, the
+ * layout of the reference's "source" dataset (src/simulation.cpp:137-175):
+ * x y z ux uy uz E wgt wgt2.  The rows become histories 0..n-1 (family id =
+ * history id), each stream seeded at its history id, and nparticles (the
+ * tallies' total weight and the bank normalisation) becomes the rounded total
+ * weight, for this and later runs of the context.  The bank is kept for
+ * every later run until cleared with n = 0.  The file itself is the caller's
+ * to read (no HDF5 here); abx_read_source_bank gives what to write. */
+int abx_set_source_bank(abx_ctx* ctx, const double* source, size_t n);
+
 /* FixedSource::run (src/fixed_source.cpp:81-173). */
 int abx_run_fixed_source(abx_ctx* ctx, int nbatches, uint64_t nparticles,
                          abx_run_stats* stats);

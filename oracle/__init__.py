@@ -38,6 +38,7 @@ def load():
             "oracle_run_power_iteration": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, P(abi.RunStats),
                                                      C.c_void_p, C.c_void_p]),
             "oracle_run_fixed_source": (C.c_int, [C.c_void_p, C.c_int, C.c_uint64, C.c_int, P(abi.RunStats)]),
+            "oracle_set_source_bank": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
             "oracle_set_trace": (C.c_int, [C.c_void_p, C.c_uint32, C.c_size_t]),
             "oracle_get_trace": (C.c_int, [C.c_void_p, P(abi.TraceRec), C.c_size_t, P(C.c_size_t)]),
             "oracle_majorant": (C.c_int, [C.c_void_p, P(C.c_double)]),
@@ -130,6 +131,11 @@ class Oracle:
         self._chk(self.lib.oracle_run_power_iteration(self.ctx, ngenerations, nignored, nthreads or self.nthreads,
                                                       C.byref(st), k.ctypes.data, h.ctypes.data))
         return stats_dict(st), k, h
+
+    def set_source_bank(self, source):
+        """Restart the next power iteration from rows x y z ux uy uz E wgt wgt2."""
+        src = np.ascontiguousarray(source, dtype=np.float64).reshape(-1, 9)
+        self._chk(self.lib.oracle_set_source_bank(self.ctx, src.ctypes.data, src.shape[0]))
 
     def run_fixed_source(self, nbatches, nparticles, nthreads=None):
         st = abi.RunStats()

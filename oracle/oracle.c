@@ -235,6 +235,8 @@ struct oracle_ctx {
   int nsrc; abx_source* src; double* src_cdf;
   /* trace */
   uint32_t tr_nhist; size_t tr_cap; size_t tr_n; abx_trace_rec* tr;
+  /* source bank to restart power iterations from ([n][9]), or NULL */
+  double* restart; size_t n_restart;
   /* status */
   int err;
 };
@@ -1686,13 +1688,50 @@ static double now_ms(void) {
 }
 
 /* PowerIterator::initialize + run (src/power_iterator.cpp:46-166, 305-473, 538-586) */
+/* PowerIterator::load_source_from_file (src/power_iterator.cpp:60-132):
+ * rows x y z ux uy uz E wgt wgt2 become histories 0..n-1 (family = history
+ * id), each stream seeded at its id; nparticles becomes the rounded total
+ * weight. */
+int oracle_set_source_bank(oracle_ctx* ctx, const double* src, size_t n) {
+  free(ctx->restart);
+  ctx->restart = NULL;
+  ctx->n_restart = 0;
+  if (n == 0) return ABX_OK;
+  ctx->restart = (double*)xcalloc(9 * n, sizeof(double));
+  memcpy(ctx->restart, src, 9 * n * sizeof(double));
+  ctx->n_restart = n;
+  return ABX_OK;
+}
+
 int oracle_run_power_iteration(oracle_ctx* ctx, int ngen, int nignored, int nthreads,
                                abx_run_stats* st, double* kcol_gen, double* ent_gen) {
-  size_t N = (size_t)ctx->set.nparticles;
-  abx_particle* bank = (abx_particle*)xcalloc(N, sizeof(abx_particle));
   double t0 = now_ms();
-  int rc = oracle_sample_sources(ctx, 0, N, bank);
-  if (rc) { free(bank); return rc; }
+  int rc;
+  abx_particle* bank;
+  size_t N;
+  if (ctx->n_restart) {
+    N = ctx->n_restart;
+    bank = (abx_particle*)xcalloc(N, sizeof(abx_particle));
+    double tot_wgt = 0.;
+    for (size_t i = 0; i < N; i++) {
+      const double* q = ctx->restart + 9 * i;
+      abx_particle* p = &bank[i];
+      memcpy(p->r, q, 3 * sizeof(double));
+      memcpy(p->u, q + 3, 3 * sizeof(double));
+      p->E = q[6]; p->wgt = q[7]; p->wgt2 = q[8];
+      p->history_id = i;
+      p->family_id = i;
+      oracle_pcg32_seed(ctx->set.seed, &p->rng_state);
+      oracle_pcg32_advance(&p->rng_state, ctx->set.stride * p->history_id);
+      tot_wgt += q[7];
+    }
+    ctx->set.nparticles = round(tot_wgt);
+  } else {
+    N = (size_t)ctx->set.nparticles;
+    bank = (abx_particle*)xcalloc(N, sizeof(abx_particle));
+    rc = oracle_sample_sources(ctx, 0, N, bank);
+    if (rc) { free(bank); return rc; }
+  }
   uint64_t global = N;
   size_t nb = N;
   double kcol = 1.0;
@@ -1895,6 +1934,7 @@ void oracle_destroy(oracle_ctx* ctx) {
   free(ctx->lat_pxi); free(ctx->lat_pyi); free(ctx->lat_pzi);
   free(ctx->cell_lists); free(ctx->lat_elems);
   free(ctx->Et); free(ctx->Eabs); free(ctx->Ef); free(ctx->nu_tot); free(ctx->nu_d);
+  free(ctx->restart);
   free(ctx->Es); free(ctx->vEf); free(ctx->ps_cdf); free(ctx->chi_cdf); free(ctx->fissile);
   if (ctx->dg_cdf) for (int m = 0; m < ctx->M; m++) { free(ctx->dg_cdf[m]); free(ctx->dg_lambda[m]); }
   free(ctx->dg_cdf); free(ctx->dg_lambda); free(ctx->n_dg);

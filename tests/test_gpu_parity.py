@@ -156,6 +156,29 @@ def test_source_bank_after_power_iteration():
         eng.read_source_bank()
 
 
+def test_restart_from_a_source_bank_matches():
+    """PowerIterator::load_source_from_file: rows x y z ux uy uz E wgt wgt2
+    become histories 0..n-1 seeded at their ids, nparticles becomes the
+    rounded total weight; the restarted power iteration matches the oracle's
+    generation by generation."""
+    b = decks.config0(nparticles=2000)
+    eng, ora, _ = pair(b, nthreads=oracle.cores())
+    eng.run_power_iteration(4, 1)
+    bank, _ = eng.read_source_bank()
+    rows = Engine.source_rows(bank)
+    rows[:, 7] *= 1.25  # total weight 2500: the restarted run normalises to it
+    eng.set_source_bank(rows)
+    ora.set_source_bank(rows)
+    sg, kg, hg = eng.run_power_iteration(5, 1)
+    sc, kc, hc = ora.run_power_iteration(5, 1)
+    assert np.allclose(kg, kc, rtol=1e-11, atol=0) and np.allclose(hg, hc, rtol=1e-11, atol=0)
+    assert sg["collisions"] == sc["collisions"] and sg["histories"] == sc["histories"]
+    nxt, _ = eng.read_source_bank()
+    assert abs(nxt["wgt"].sum() - 2500.0) <= 1e-9 * 2500.0
+    eng.set_source_bank(None)  # back to sampling the problem's sources
+    eng.run_power_iteration(2, 1)
+
+
 def test_fixed_source_matches():
     b = decks.fixed_source_problem(0, nparticles=3000, precision="fp64")
     eng, ora, _ = pair(b, nthreads=oracle.cores())
