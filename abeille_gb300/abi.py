@@ -27,7 +27,7 @@ QUANTITY = {"flux": 0, "elastic": 1, "absorption": 2, "fission": 3, "total": 4}
 SPATIAL = {"point": 0, "box": 1}
 DIRECTION = {"isotropic": 0, "mono-directional": 1}
 MODE = {"k-eigenvalue": 0, "fixed-source": 1, "branchless-k-eigenvalue": 0}  # the last with BRANCHLESS_ON
-BRANCHLESS_ON, BRANCHLESS_MATERIAL, BRANCHLESS_SPLITTING = 1, 2, 4
+BRANCHLESS_ON, BRANCHLESS_MATERIAL, BRANCHLESS_SPLITTING, BRANCHLESS_COMBING = 1, 2, 4, 8
 TRACKING = {"delta-tracking": 0, "surface-tracking": 1, "implicit-leakage-delta-tracking": 2,
             "carter-tracking": 3}
 PRECISION = {"fp64": 0, "mixed": 1}
@@ -82,7 +82,7 @@ class Settings(C.Structure):
                 ("seed", C.c_uint64), ("stride", C.c_uint64), ("wgt_cutoff", C.c_double),
                 ("wgt_survival", C.c_double), ("nparticles", C.c_double), ("block_size", C.c_int32),
                 ("reserved", C.c_int32), ("wgt_split", C.c_double), ("branchless", C.c_int32),
-                ("reserved2", C.c_int32)]
+                ("global_rng_skip", C.c_int32)]
 
 
 class Problem(C.Structure):

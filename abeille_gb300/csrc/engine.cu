@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
+#include <random>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -479,7 +481,8 @@ static int append_problem(Pools& P, const abx_problem* pr) {
     return fail(ABX_ERR_INVALID, "wgt-split must exceed wgt-survival (src/parser.cpp:689-697)");
   pt.branchless = 0;
   if (s.branchless) {
-    if (s.branchless & ~(ABX_BRANCHLESS_ON | ABX_BRANCHLESS_MATERIAL | ABX_BRANCHLESS_SPLITTING) ||
+    if (s.branchless & ~(ABX_BRANCHLESS_ON | ABX_BRANCHLESS_MATERIAL | ABX_BRANCHLESS_SPLITTING |
+                         ABX_BRANCHLESS_COMBING) ||
         !(s.branchless & ABX_BRANCHLESS_ON))
       return fail(ABX_ERR_INVALID, "branchless flags %d", s.branchless);
     if (s.mode != ABX_MODE_K_EIGENVALUE)
@@ -487,6 +490,7 @@ static int append_problem(Pools& P, const abx_problem* pr) {
     if (s.tracking != ABX_TRACK_DELTA && s.tracking != ABX_TRACK_SURFACE)
       return fail(ABX_ERR_UNSUPPORTED, "branchless collisions with delta or surface tracking only");
     pt.branchless = s.branchless;
+    pt.global_rng_skip = s.global_rng_skip;
   }
   pt.nparticles = s.nparticles;
   pt.inv_np = 1. / s.nparticles;
@@ -908,7 +912,8 @@ __global__ void k_next_bank(SiteT<R> S, DevState* st, const uint32_t* off, BankT
   // normalize_weights (src/power_iterator.cpp:538-586): N over the bank's net
   // weight, sites of weight +-1 unless the collisions are branchless
   const double W = P.branchless ? st->site_wsum : (double)st->site_pos - (double)st->site_neg;
-  const double wpp = P.nparticles / W;
+  // a combed bank is normalised on the host, in the reference's summation order
+  const double wpp = (P.branchless & ABX_BRANCHLESS_COMBING) ? 1. : P.nparticles / W;
   const unsigned long long g0 = run->global_hist;
   double w_in_mesh = 0.;  // this thread's share of the entropy total
   for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < ns && j < cap;
@@ -1778,14 +1783,10 @@ extern "C" int abx_tally_read_all(abx_ctx* c, double* avg, double* var, size_t c
   return ABX_OK;
 }
 
-extern "C" int abx_entropy(abx_ctx* c, const abx_site* s, size_t n, double* H) {
-  // Entropy::add_point + calculate_entropy (src/entropy.cpp:32-93), Sign::Total, FP64.
-  if (!c || !H || (!s && n)) return fail(ABX_ERR_INVALID, "bad arguments");
-  const ProbT& P = c->prob0;
-  if (!P.ent_on) {
-    *H = 0.;
-    return ABX_OK;
-  }
+// Entropy::add_point + calculate_entropy (src/entropy.cpp:32-93), Sign::Total,
+// FP64, over n points of any record with r[3] and wgt.
+template <class Pt> static double entropy_of(const ProbT& P, const Pt* s, size_t n) {
+  if (!P.ent_on) return 0.;
   size_t nb = (size_t)P.ent_shape[0] * P.ent_shape[1] * P.ent_shape[2];
   std::vector<double> bins(nb, 0.);
   double tw = 0.;
@@ -1806,7 +1807,12 @@ extern "C" int abx_entropy(abx_ctx* c, const abx_site* s, size_t n, double* H) {
       sum -= p * std::log2(p);
     }
   }
-  *H = sum;
+  return sum;
+}
+
+extern "C" int abx_entropy(abx_ctx* c, const abx_site* s, size_t n, double* H) {
+  if (!c || !H || (!s && n)) return fail(ABX_ERR_INVALID, "bad arguments");
+  *H = entropy_of(c->prob0, s, n);
   return ABX_OK;
 }
 
@@ -1959,6 +1965,114 @@ extern "C" int abx_set_graphs(abx_ctx* c, int enabled) {
   return ABX_OK;
 }
 
+// The reference's global stream (settings::rng, a pcg32) on the host, as a
+// uniform random bit generator for libstdc++'s std::shuffle and
+// uniform_real_distribution, the calls BranchlessPowerIterator makes.
+struct GlobalStream {
+  using result_type = uint32_t;
+  uint64_t state;
+  static constexpr result_type min() { return 0u; }
+  static constexpr result_type max() { return 0xffffffffu; }
+  result_type operator()() {
+    const uint64_t old = state;
+    state = old * PCG_MULT + PCG_INC;
+    const uint32_t rot = (uint32_t)(old >> 59);
+    const uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+  }
+};
+
+// The host half of a branchless generation with combing, after the device
+// wrote the next bank (unnormalised, in the reference's order) into bank
+// `nxt`: BranchlessPowerIterator::normalize_weights and comb_particles
+// (src/branchless_power_iterator.cpp:541-650), then the bank rebuilt as
+// PowerIterator does (new history ids in order, streams seeded at them,
+// src/branchless_power_iterator.cpp:415-423) and the entropy of the combed
+// bank (compute_post_cancellation_entropy) put in the generation's record.
+static int comb_generation(abx_ctx* c, bool mixed, int nxt, int g, GlobalStream& gs, size_t cap) {
+  int rc;
+  if ((rc = check_state(c)) != ABX_OK) return rc;
+  const size_t ns = (size_t)c->st_host->n_hist;
+  std::vector<abx_particle> bank(ns);
+  if (c->aos_in_cap < std::max(ns, cap)) {
+    if (c->aos_in) cudaFree(c->aos_in);
+    c->aos_in = nullptr;
+    c->aos_in_cap = 0;
+    CUDA_TRY(cudaMalloc(&c->aos_in, std::max(ns, cap) * sizeof(abx_particle)));
+    c->aos_in_cap = std::max(ns, cap);
+  }
+  if (ns) {
+    if (mixed) k_bank_to_aos<float><<<grid_for(ns), 256, 0, c->stream>>>(c->bf[nxt].b, ns, c->aos_in);
+    else k_bank_to_aos<double><<<grid_for(ns), 256, 0, c->stream>>>(c->bd[nxt].b, ns, c->aos_in);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(bank.data(), c->aos_in, ns * sizeof(abx_particle), cudaMemcpyDeviceToHost, c->stream));
+  }
+  RunAcc ra;
+  CUDA_TRY(cudaMemcpyAsync(&ra, c->run, sizeof ra, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  // normalize_weights
+  double W_pos = 0., W_neg = 0.;
+  for (const abx_particle& p : bank) {
+    if (p.wgt > 0.) W_pos += p.wgt;
+    else W_neg -= p.wgt;
+  }
+  const double wpp = c->prob0.nparticles / (W_pos - W_neg);
+  for (abx_particle& p : bank) p.wgt *= wpp;
+  // comb_particles: only positive weights occur with branchless collisions
+  std::vector<abx_particle> pos;
+  pos.reserve(ns);
+  double Wpos = 0.;
+  for (const abx_particle& p : bank) {
+    if (!(p.wgt > 0.)) return fail(ABX_ERR_UNSUPPORTED, "combing a bank with non-positive weights");
+    Wpos += p.wgt;
+    pos.push_back(p);
+  }
+  const size_t Npos = (size_t)std::ceil(Wpos);
+  std::shuffle(pos.begin(), pos.end(), gs);
+  std::uniform_real_distribution<double> unit(0., 1.);  // RNG::rand (include/utils/rng.hpp:41)
+  const double avg_pos = Wpos / (double)Npos;
+  double comb_pos = unit(gs) * avg_pos;
+  double current = 0.;
+  std::vector<abx_particle> next;
+  next.reserve(Npos + 4);
+  for (const abx_particle& p : pos) {
+    current += p.wgt;
+    while (comb_pos < current) {
+      next.push_back(p);
+      next.back().wgt = avg_pos;
+      comb_pos += avg_pos;
+    }
+  }
+  (void)unit(gs);  // the comb position of the (empty) negative part
+  std::shuffle(next.begin(), next.end(), gs);
+  const size_t m = next.size();
+  if (m == 0) return fail(ABX_ERR_NO_FISSION, "No fission neutrons were produced.");
+  if (m > cap) return fail(ABX_ERR_CAPACITY, "combed bank of %zu particles, capacity %zu", m, cap);
+  // the next generation's particles: history ids from the global counter
+  const uint64_t base = ra.global_hist - ns;
+  for (size_t i = 0; i < m; i++) {
+    abx_particle& p = next[i];
+    p.wgt2 = 0.;
+    p.history_id = base + i;
+    p.rng_state = pcg_advance(pcg_seeded(c->prob0.seed), c->prob0.stride * p.history_id);
+  }
+  ra.global_hist = base + m;
+  const double H = entropy_of(c->prob0, next.data(), m);
+  CUDA_TRY(cudaMemcpyAsync(c->aos_in, next.data(), m * sizeof(abx_particle), cudaMemcpyHostToDevice, c->stream));
+  if (mixed) k_bank_from_aos<float><<<grid_for(m), 256, 0, c->stream>>>(c->aos_in, m, c->bf[nxt].b);
+  else k_bank_from_aos<double><<<grid_for(m), 256, 0, c->stream>>>(c->aos_in, m, c->bd[nxt].b);
+  CUDA_TRY(cudaGetLastError());
+  const unsigned long long n_hist = m;
+  CUDA_TRY(cudaMemcpyAsync((char*)c->st + offsetof(DevState, n_hist), &n_hist, sizeof n_hist,
+                           cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync((char*)c->run + offsetof(RunAcc, global_hist), &ra.global_hist,
+                           sizeof ra.global_hist, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync((char*)(c->gen_rec + (g - 1)) + offsetof(abx_gen_record, entropy), &H, sizeof H,
+                           cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));  // host vectors are pageable and go out of scope
+  return ABX_OK;
+}
+
 // PowerIterator::load_source_from_file (src/power_iterator.cpp:60-132): the
 // stored particles become histories 0..n-1 (family = history id), each
 // stream seeded at its id.  The caller has already set nparticles to the
@@ -2079,7 +2193,11 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
   const std::vector<cudaEvent_t> evs(c->ev_pool.begin(), c->ev_pool.begin() + 4 * (size_t)ngen);
   int cur = 0;
   int active_tally = 0;
-  const bool graphs = c->use_graphs && c->trace_nhist == 0;
+  // branchless combing: a host step after every generation, so no graphs;
+  // its stream starts as a default-constructed pcg32 after the deck's draws
+  const bool combing = (c->prob0.branchless & ABX_BRANCHLESS_COMBING) != 0;
+  GlobalStream gs{pcg_advance(pcg_seeded(0xcafef00dd15ea5e5ULL), (uint64_t)std::max(0, c->prob0.global_rng_skip))};
+  const bool graphs = c->use_graphs && c->trace_nhist == 0 && !combing;
   if (graphs && (rc = ensure_gen_graphs(c, mixed, cap, nignored)) != ABX_OK) return rc;
   for (int g = 1; g <= ngen; g++) {
     if (c->flush_bytes) CUDA_TRY(cudaMemsetAsync(c->flush, g & 0xff, c->flush_bytes, c->stream));
@@ -2099,6 +2217,7 @@ extern "C" int abx_run_power_iteration_ex(abx_ctx* c, int ngen, int nignored, ab
     cudaEventRecord(evs[4 * (g - 1) + 3], c->stream);
     CUDA_TRY(cudaGetLastError());
     cur = 1 - cur;
+    if (combing && (rc = comb_generation(c, mixed, cur, g, gs, cap)) != ABX_OK) break;
     if ((g & 7) == 0 || g == ngen) {
       if ((rc = check_state(c)) != ABX_OK) break;
     }

@@ -91,7 +91,7 @@ struct ProbT {
   float wgt_split_f;
   double wgt_split;               // Carter tracking and branchless splitting split at |weight| >= this
   int32_t branchless;             // ABX_BRANCHLESS_* flags (0: branching collisions)
-  int32_t pad2_;
+  int32_t global_rng_skip;        // combing: outputs the global stream drew before the run
 };
 
 struct Tables {

@@ -282,11 +282,16 @@ def from_reference_deck(deck, nparticles=None, precision="fp64", tracking=None):
                        wgt_cutoff=float(st.get("wgt-cutoff", 0.25)), wgt_survival=float(st.get("wgt-survival", 1.0)),
                        wgt_split=float(st.get("wgt-split", 2.0)), sampling_xs_ratio=deck.get("sampling-xs-ratio"),
                        branchless_material=bool(st.get("branchless-material", True)),
-                       branchless_splitting=bool(st.get("branchless-splitting", False)))
-    if st["simulation"] == "branchless-k-eigenvalue" and st.get("branchless-combing", True):
-        # BranchlessPowerIterator::comb_particles (src/branchless_power_iterator.cpp:592-650),
-        # the reference's default, shuffles the bank with the global stream
-        raise ValueError("branchless-combing is not supported: set branchless-combing: false")
+                       branchless_splitting=bool(st.get("branchless-splitting", False)),
+                       branchless_combing=bool(st.get("branchless-combing", True)),
+                       # the global stream draws a plot colour for every cell and every
+                       # material without one while the deck is read (src/cell.cpp:445-448,
+                       # src/material.cpp:440-449): 3 canonical draws of 2 outputs each
+                       global_rng_skip=6 * (len(deck["cells"]) + sum(
+                           1 for m in deck["materials"]
+                           if not (isinstance(m.get("color"), list) and len(m["color"]) == 3))))
+    if st.get("regional-cancellation", False):
+        raise ValueError("regional cancellation is outside the multigroup transport path")
     for m in deck["materials"]:
         leg = {l: m[f"P{l}"] for l in range(1, 6) if f"P{l}" in m}
         b.material(int(m["id"]), total=m["total"], absorption=m["absorption"], scatter=m["scatter"],

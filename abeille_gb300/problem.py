@@ -99,7 +99,8 @@ class ProblemBuilder:
     def __init__(self, ngroups, energy_bounds, mode="k-eigenvalue", tracking="delta-tracking",
                  precision="fp64", nparticles=10000, seed=19073486328125, stride=152917,
                  wgt_cutoff=0.25, wgt_survival=1.0, block_size=0, wgt_split=2.0, sampling_xs_ratio=None,
-                 branchless_material=True, branchless_splitting=False):
+                 branchless_material=True, branchless_splitting=False, branchless_combing=True,
+                 global_rng_skip=None):
         self.G = int(ngroups)
         self.energy_bounds = np.asarray(energy_bounds, dtype=np.float64)
         if self.energy_bounds.shape != (self.G + 1,):
@@ -112,6 +113,11 @@ class ProblemBuilder:
         # BranchlessPowerIterator (settings branchless-material / -splitting,
         # defaults as src/settings.cpp:87-89)
         self.branchless_material, self.branchless_splitting = bool(branchless_material), bool(branchless_splitting)
+        self.branchless_combing = bool(branchless_combing)
+        # outputs the reference's global stream draws while reading the deck
+        # (plot colours: 6 per cell and per material without one); None: 6 per
+        # cell and per material of this builder
+        self.global_rng_skip = global_rng_skip
         self.sampling_xs_ratio = None if sampling_xs_ratio is None else [float(x) for x in sampling_xs_ratio]
         self.surfaces, self.cells, self.universes, self.materials = [], [], {}, []
         self.universe_decl = []
@@ -299,6 +305,7 @@ class ProblemBuilder:
         if self.mode == "branchless-k-eigenvalue":
             settings["branchless-material"] = self.branchless_material
             settings["branchless-splitting"] = self.branchless_splitting
+            settings["branchless-combing"] = self.branchless_combing
         if ngenerations is not None:
             settings["ngenerations"] = int(ngenerations)
         if nignored is not None:
@@ -440,7 +447,10 @@ class ProblemBuilder:
         s.branchless = 0
         if self.mode == "branchless-k-eigenvalue":
             s.branchless = (abi.BRANCHLESS_ON | (abi.BRANCHLESS_MATERIAL if self.branchless_material else 0) |
-                            (abi.BRANCHLESS_SPLITTING if self.branchless_splitting else 0))
+                            (abi.BRANCHLESS_SPLITTING if self.branchless_splitting else 0) |
+                            (abi.BRANCHLESS_COMBING if self.branchless_combing else 0))
+            s.global_rng_skip = (self.global_rng_skip if self.global_rng_skip is not None
+                                 else 6 * (len(self.cells) + len(self.materials)))
         p.energy_bounds = _ptr(eb, C.c_double)
         p.surfaces = C.cast(surf, C.POINTER(abi.Surface))
         p.n_surfaces = len(self.surfaces)

@@ -207,7 +207,11 @@ typedef struct abx_settings {
   int32_t branchless; /* ABX_BRANCHLESS_* flags; non-zero with
                          ABX_MODE_K_EIGENVALUE = the reference's
                          branchless-k-eigenvalue simulation               */
-  int32_t reserved2;
+  int32_t global_rng_skip; /* combing: pcg32 outputs the reference's global
+                         stream (settings::rng, src/settings.cpp:59) has
+                         drawn before the run -- 6 per cell and per material
+                         without a colour (random plot colours,
+                         src/cell.cpp:445-448, src/material.cpp:444-449) */
 } abx_settings;
 
 /* Branchless collisions (Transporter::branchless_collision,
@@ -219,11 +223,15 @@ typedef struct abx_settings {
  * that weight.  ON selects the per-nuclide form (branchless_collision_iso),
  * ON | MATERIAL the per-material one (settings branchless-material),
  * SPLITTING splits particles whose |weight| reaches wgt_split (settings
- * branchless-splitting).  The reference's bank combing and regional
- * cancellation are not part of this path (the deck reader refuses
- * branchless-combing).  Delta and surface tracking only; abx_create returns
- * ABX_ERR_UNSUPPORTED for other combinations. */
-enum { ABX_BRANCHLESS_ON = 1, ABX_BRANCHLESS_MATERIAL = 2, ABX_BRANCHLESS_SPLITTING = 4 };
+ * branchless-splitting), COMBING combs the normalised bank every generation
+ * (settings branchless-combing, BranchlessPowerIterator::comb_particles,
+ * src/branchless_power_iterator.cpp:592-650: std::shuffle and a comb of
+ * ceil(W) equal weights drawn from the global stream, on the host between
+ * generations).  Regional cancellation is not part of this path.  Delta and
+ * surface tracking only; abx_create returns ABX_ERR_UNSUPPORTED for other
+ * combinations. */
+enum { ABX_BRANCHLESS_ON = 1, ABX_BRANCHLESS_MATERIAL = 2, ABX_BRANCHLESS_SPLITTING = 4,
+       ABX_BRANCHLESS_COMBING = 8 };
 
 /* ------------------------------------------------------------- problem */
 typedef struct abx_problem {

@@ -39,6 +39,7 @@ def load():
                                                      C.c_void_p, C.c_void_p]),
             "oracle_run_fixed_source": (C.c_int, [C.c_void_p, C.c_int, C.c_uint64, C.c_int, P(abi.RunStats)]),
             "oracle_set_source_bank": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+            "oracle_shuffle": (None, [C.c_void_p, C.c_size_t, C.c_size_t, P(C.c_uint64)]),
             "oracle_set_trace": (C.c_int, [C.c_void_p, C.c_uint32, C.c_size_t]),
             "oracle_get_trace": (C.c_int, [C.c_void_p, P(abi.TraceRec), C.c_size_t, P(C.c_size_t)]),
             "oracle_majorant": (C.c_int, [C.c_void_p, P(C.c_double)]),

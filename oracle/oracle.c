@@ -135,6 +135,64 @@ double oracle_canonical(uint64_t* st) {
   if (ret >= 1.0) ret = 0x1.fffffffffffffp-1; /* nextafter(1, 0) */
   return ret;
 }
+/* libstdc++ uniform_int_distribution<unsigned long>{0, range} over a 32-bit
+ * engine (bits/uniform_int_dist.h): for range < 2^32 - 1 the engine's range
+ * is larger, and the draw is Lemire's nearly divisionless method (D. Lemire,
+ * "Fast random integer generation in an interval", ACM TOMACS 29(1), 2019)
+ * on 64-bit products: the high half of output * (range + 1), redrawn while
+ * the low half falls below 2^32 mod (range + 1).  Ranges of 2^32 - 1 or more
+ * (banks of four billion particles) are not needed here. */
+static uint64_t uniform_upto(uint64_t* st, uint64_t range) {
+  const uint32_t uerange = (uint32_t)(range + 1u);
+  uint64_t product = (uint64_t)oracle_pcg32_next(st) * (uint64_t)uerange;
+  uint32_t low = (uint32_t)product;
+  if (low < uerange) {
+    const uint32_t threshold = (uint32_t)(0u - uerange) % uerange;
+    while (low < threshold) {
+      product = (uint64_t)oracle_pcg32_next(st) * (uint64_t)uerange;
+      low = (uint32_t)product;
+    }
+  }
+  return product >> 32;
+}
+
+/* std::shuffle over a 32-bit engine (libstdc++ bits/stl_algo.h): when
+ * n * n fits the engine's range (n <= 65535) the swap positions of two
+ * successive elements come from one draw over [0, (i+1)(i+2)), an even n
+ * first swapping element 1 with a draw over [0, 1]; otherwise one draw over
+ * [0, i] per element i = 1 .. n-1. */
+static void swap_elems(unsigned char* base, size_t sz, size_t i, size_t j, unsigned char* tmp) {
+  if (i == j) return;
+  memcpy(tmp, base + i * sz, sz);
+  memcpy(base + i * sz, base + j * sz, sz);
+  memcpy(base + j * sz, tmp, sz);
+}
+void oracle_shuffle(void* data, size_t n, size_t sz, uint64_t* st) {
+  if (n == 0) return;
+  unsigned char* base = (unsigned char*)data;
+  unsigned char* tmp = (unsigned char*)calloc(1, sz ? sz : 1);
+  if (!tmp) return;
+  const uint64_t urngrange = 0xffffffffULL, urange = n;
+  if (urngrange / urange >= urange) {
+    size_t i = 1;
+    if ((urange % 2) == 0) {
+      swap_elems(base, sz, i, (size_t)uniform_upto(st, 1), tmp);
+      i++;
+    }
+    while (i != n) {
+      const uint64_t swap_range = (uint64_t)i + 1;
+      const uint64_t x = uniform_upto(st, swap_range * (swap_range + 1) - 1);
+      swap_elems(base, sz, i, (size_t)(x / (swap_range + 1)), tmp);
+      i++;
+      swap_elems(base, sz, i, (size_t)(x % (swap_range + 1)), tmp);
+      i++;
+    }
+  } else {
+    for (size_t i = 1; i < n; i++) swap_elems(base, sz, i, (size_t)uniform_upto(st, i), tmp);
+  }
+  free(tmp);
+}
+
 /* RNG::exponential (include/utils/rng.hpp:72-77) + exponential_distribution */
 double oracle_exponential(uint64_t* st, double lambda) {
   if (lambda == 0.) return INF_;
@@ -1688,6 +1746,56 @@ static double now_ms(void) {
 }
 
 /* PowerIterator::initialize + run (src/power_iterator.cpp:46-166, 305-473, 538-586) */
+/* BranchlessPowerIterator::comb_particles (src/branchless_power_iterator.cpp:
+ * 592-650) on the normalised bank: positive and negative sites apart, each
+ * shuffled with the global stream and combed into ceil(W) sites of equal
+ * weight (a comb position drawn in [0, W/N) then steps of W/N), the result
+ * shuffled again.  Negative weights do not occur with branchless collisions
+ * alone; a bank holding some is refused. */
+static int comb_sites(abx_site** psites, size_t* pn, uint64_t* gs) {
+  abx_site* s = *psites;
+  const size_t n = *pn;
+  abx_site* pos = (abx_site*)xcalloc(n, sizeof(abx_site));
+  size_t np = 0;
+  double Wpos = 0., Wneg = 0.;
+  for (size_t i = 0; i < n; i++) {
+    if (s[i].wgt > 0.) { Wpos += s[i].wgt; pos[np++] = s[i]; }
+    else Wneg += s[i].wgt;
+  }
+  if (np != n) { free(pos); set_err("combing a bank with non-positive weights"); return ABX_ERR_UNSUPPORTED; }
+  const size_t Npos = (size_t)ceil(Wpos);
+  oracle_shuffle(pos, np, sizeof(abx_site), gs);
+  const double avg_pos = Wpos / (double)Npos;
+  double comb_pos = oracle_canonical(gs) * avg_pos;
+  double cur = 0.;
+  size_t cap = Npos + 4, m = 0;
+  abx_site* out = (abx_site*)xcalloc(cap, sizeof(abx_site));
+  for (size_t i = 0; i < np; i++) {
+    cur += pos[i].wgt;
+    while (comb_pos < cur) {
+      if (m == cap) {
+        cap *= 2;
+        abx_site* nv = (abx_site*)realloc(out, cap * sizeof(abx_site));
+        if (!nv) { free(out); free(pos); set_err("out of memory"); return ABX_ERR_OOM; }
+        out = nv;
+      }
+      out[m] = pos[i];
+      out[m].wgt = avg_pos;
+      m++;
+      comb_pos += avg_pos;
+    }
+  }
+  /* the negative sites: none to shuffle or comb, but the comb position is drawn */
+  (void)oracle_canonical(gs);
+  (void)Wneg;
+  oracle_shuffle(out, m, sizeof(abx_site), gs);
+  free(pos);
+  free(s);
+  *psites = out;
+  *pn = m;
+  return ABX_OK;
+}
+
 /* PowerIterator::load_source_from_file (src/power_iterator.cpp:60-132):
  * rows x y z ux uy uz E wgt wgt2 become histories 0..n-1 (family = history
  * id), each stream seeded at its id; nparticles becomes the rounded total
@@ -1734,6 +1842,12 @@ int oracle_run_power_iteration(oracle_ctx* ctx, int ngen, int nignored, int nthr
   }
   uint64_t global = N;
   size_t nb = N;
+  /* the global stream the combing draws from: a default-constructed pcg32
+   * (src/settings.cpp:59) after the draws made while the deck was read */
+  const int combing = (ctx->set.branchless & ABX_BRANCHLESS_COMBING) != 0;
+  uint64_t gstream;
+  oracle_pcg32_seed(0xcafef00dd15ea5e5ULL, &gstream);
+  oracle_pcg32_advance(&gstream, (uint64_t)(ctx->set.global_rng_skip > 0 ? ctx->set.global_rng_skip : 0));
   double kcol = 1.0;
   int converged = nignored == 0;
   int active = 0;
@@ -1753,7 +1867,7 @@ int oracle_run_power_iteration(oracle_ctx* ctx, int ngen, int nignored, int nthr
     if (rc) { free(sites); free(bank); return rc; }
     S.collisions += sc.collisions; S.flights += sc.flights; S.histories += nb;
     if (ns == 0) { free(sites); free(bank); set_err("No fission neutrons were produced."); return ABX_ERR_NO_FISSION; }
-    if (ent_gen) { double H; oracle_entropy(ctx, sites, ns, &H); ent_gen[g - 1] = H; }
+    if (ent_gen && !combing) { double H; oracle_entropy(ctx, sites, ns, &H); ent_gen[g - 1] = H; }
     double tw = ctx->set.nparticles;
     double k_col = sc.k_col / tw, k_abs = sc.k_abs / tw, k_trk = sc.k_trk / tw;
     double leak = sc.leakage / tw, mig = sc.mig_area / tw;
@@ -1767,6 +1881,12 @@ int oracle_run_power_iteration(oracle_ctx* ctx, int ngen, int nignored, int nthr
     double W = W_pos - W_neg;
     double wpp = (double)ctx->set.nparticles / W;
     for (size_t i = 0; i < ns; i++) sites[i].wgt *= wpp;
+    if (combing) {
+      rc = comb_sites(&sites, &ns, &gstream);
+      if (rc) { free(sites); free(bank); return rc; }
+      /* the entropy of the combed bank (compute_post_cancellation_entropy) */
+      if (ent_gen) { double H; oracle_entropy(ctx, sites, ns, &H); ent_gen[g - 1] = H; }
+    }
     if (converged) {
       active++;
       update_avg_var(active, k_col, &kcol_avg, &kcol_var);

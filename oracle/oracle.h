@@ -47,6 +47,7 @@ int oracle_run_power_iteration(oracle_ctx* ctx, int ngenerations, int nignored,
                                int nthreads, abx_run_stats* stats,
                                double* kcol_per_gen, double* entropy_per_gen);
 int oracle_set_source_bank(oracle_ctx* ctx, const double* source, size_t n);
+void oracle_shuffle(void* data, size_t n, size_t elem_size, uint64_t* state);
 int oracle_run_fixed_source(oracle_ctx* ctx, int nbatches, uint64_t nparticles,
                             int nthreads, abx_run_stats* stats);
 int oracle_set_trace(oracle_ctx* ctx, uint32_t n_hist, size_t capacity);

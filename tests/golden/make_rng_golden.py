@@ -12,7 +12,10 @@ and the system libstdc++ -- and records what they produce:
   * ``std::uniform_real_distribution<double>(0,1)`` (== RNG::rand);
   * ``std::exponential_distribution<double>``;
   * ``std::discrete_distribution<int>`` on several weight vectors, followed by
-    one more canonical draw to show how many outputs each sample consumed.
+    one more canonical draw to show how many outputs each sample consumed;
+  * the state of a default-constructed ``pcg32`` (settings::rng) and
+    ``std::shuffle`` of 1 .. 70001 elements (checksum, first elements and the
+    next output), as the branchless power iteration's combing uses them.
 
 Run it where pyarrow and g++ are installed; it rewrites rng_golden.json next
 to this file.  The tests read only the JSON.
@@ -31,6 +34,7 @@ CPP = r"""
 #include <random>
 #include <sstream>
 #include <vector>
+#include <algorithm>
 #include "pcg_random.hpp"
 using pcg32 = arrow_vendored::pcg32;
 
@@ -111,6 +115,30 @@ int main() {
       for (int i = 0; i < 32; i++) std::printf("%s%d", i ? ", " : "", D(r));
       std::uniform_real_distribution<double> U2(0., 1.);
       std::printf("], \"next\": \"%a\"}\n", U2(r));
+    }
+    std::printf("],\n");
+  }
+  {
+    // settings::rng (src/settings.cpp:59) is a default-constructed pcg32
+    pcg32 d;
+    std::printf("\"default_state\": %llu,\n", (unsigned long long)state_of(d));
+    // std::shuffle over a pcg32, as BranchlessPowerIterator::comb_particles
+    // uses it (src/branchless_power_iterator.cpp:619-650): both of
+    // libstdc++'s paths (swap positions drawn in pairs up to 65535 elements,
+    // one at a time above)
+    const size_t sizes[] = {1, 2, 3, 4, 7, 10, 101, 65535, 65536, 70001};
+    std::printf("\"shuffle\": [\n");
+    for (int k = 0; k < 10; k++) {
+      const size_t n = sizes[k];
+      pcg32 r(5ULL + k);
+      std::vector<uint32_t> v(n);
+      for (size_t i = 0; i < n; i++) v[i] = (uint32_t)i;
+      std::shuffle(v.begin(), v.end(), r);
+      unsigned long long check = 0;
+      for (size_t i = 0; i < n; i++) check = check * 1000003ULL + v[i];
+      std::printf("%s{\"n\": %zu, \"seed\": %d, \"head\": [", k ? "," : "", n, 5 + k);
+      for (size_t i = 0; i < n && i < 12; i++) std::printf("%s%u", i ? ", " : "", v[i]);
+      std::printf("], \"check\": %llu, \"next\": %u}\n", check, (unsigned)r());
     }
     std::printf("]\n");
   }

@@ -19,10 +19,10 @@ DECKS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "refere
 FLAVOURS = [(True, False), (False, False), (True, True), (False, True)]  # (per material, splitting)
 
 
-def _config0(n, tracking, material, splitting):
+def _config0(n, tracking, material, splitting, combing=False):
     b = decks.config0(nparticles=n, tracking=tracking)
     b.mode = "branchless-k-eigenvalue"
-    b.branchless_material, b.branchless_splitting = material, splitting
+    b.branchless_material, b.branchless_splitting, b.branchless_combing = material, splitting, combing
     return b
 
 
@@ -58,9 +58,13 @@ def test_branchless_traces_and_step_match(tracking, material, splitting):
     eng.close()
 
 
-@pytest.mark.parametrize("material,splitting", [(True, False), (False, True)])
-def test_branchless_power_iteration_matches(material, splitting):
-    b = _config0(2000, "delta-tracking", material, splitting)
+@pytest.mark.parametrize("material,splitting,combing", [(True, False, False), (False, True, False),
+                                                       (True, False, True), (False, True, True)])
+def test_branchless_power_iteration_matches(material, splitting, combing):
+    """Generation by generation against the oracle; with combing the bank is
+    normalised, combed (std::shuffle over the global stream, against the
+    oracle's restatement pinned to libstdc++) and re-numbered on the host."""
+    b = _config0(2000, "delta-tracking", material, splitting, combing)
     built = b.build(precision="fp64")
     eng, ora = Engine(built, 0), oracle.Oracle(built, nthreads=oracle.cores())
     sg, kg, hg = eng.run_power_iteration(6, 2)
@@ -75,14 +79,17 @@ def test_branchless_power_iteration_matches(material, splitting):
 
 @pytest.mark.parametrize("name,precision,material,splitting,tracking", [
     ("PUa-1-0-IN", "fp64", True, False, "delta-tracking"), ("PUa-1-0-IN", "mixed", False, True, "delta-tracking"),
-    ("PUb-1-0-SL", "mixed", True, True, "surface-tracking"), ("PUb-1-0-IN", "fp64", False, False, "surface-tracking")])
+    ("PUb-1-0-SL", "mixed", True, True, "surface-tracking"), ("PUb-1-0-IN", "fp64", False, False, "surface-tracking"),
+    ("PUa-1-0-SL", "mixed", True, None, "delta-tracking"), ("PUb-1-0-SL", "fp64", False, None, "surface-tracking")])
 def test_branchless_analytic_k_on_gpu(name, precision, material, splitting, tracking):
     """Without combing a history ends in at most one fission site unless it
     splits, so a leaking system (the slabs) needs splitting to keep its
-    population; the infinite media keep theirs without."""
+    population; the infinite media keep theirs without.  splitting None: the
+    reference's default, combing on and no splitting."""
     deck = json.loads(json.dumps(DECKS[name]))
-    deck["settings"].update({"simulation": "branchless-k-eigenvalue", "branchless-combing": False,
-                             "branchless-material": material, "branchless-splitting": splitting})
+    deck["settings"].update({"simulation": "branchless-k-eigenvalue", "branchless-material": material})
+    if splitting is not None:
+        deck["settings"].update({"branchless-combing": False, "branchless-splitting": splitting})
     b = decks.from_reference_deck(deck, nparticles=100000, tracking=tracking)
     eng = Engine(b.build(precision=precision), 0)
     st, _, _ = eng.run_power_iteration(40, 10)

@@ -85,11 +85,19 @@ def test_branchless_collisions_analytic_k(name, material, splitting, tracking):
     assert abs(st["kcol_avg"] - DECKS[name]["_expected_k"]) < 4 * st["kcol_std"] + 1e-4, st
 
 
-def test_branchless_combing_is_refused():
-    deck = json.loads(json.dumps(DECKS["PUa-1-0-IN"]))
-    deck["settings"]["simulation"] = "branchless-k-eigenvalue"
-    with pytest.raises(ValueError):
-        decks.from_reference_deck(deck, nparticles=1000)
+@pytest.mark.parametrize("name,material", [("PUa-1-0-IN", True), ("PUb-1-0-SL", False), ("PUa-1-0-SL", True)])
+def test_branchless_combing_analytic_k(name, material):
+    """The reference's default branchless simulation: the normalised bank is
+    combed every generation (shuffled with the global stream, ceil(W) equal
+    weights), which keeps the population of a leaking system without
+    splitting."""
+    deck = json.loads(json.dumps(DECKS[name]))
+    deck["settings"].update({"simulation": "branchless-k-eigenvalue", "branchless-material": material})
+    b = decks.from_reference_deck(deck, nparticles=20000, tracking="delta-tracking")
+    assert b.branchless_combing and b.global_rng_skip == 6 * (len(deck["cells"]) + len(deck["materials"]))
+    st, _, _ = oracle.Oracle(b.build(), nthreads=oracle.cores()).run_power_iteration(50, 10)
+    assert abs(st["kcol_avg"] - DECKS[name]["_expected_k"]) < 4 * st["kcol_std"] + 1e-4, st
+    assert st["histories"] / 50 == pytest.approx(20000, rel=0.01)  # ceil(W) particles per generation
 
 
 @pytest.mark.parametrize("name", ["Ua-1-1-CY", "UD2O-2-1-SL"])

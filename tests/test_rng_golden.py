@@ -4,6 +4,8 @@ import ctypes as C
 import json
 import os
 
+import numpy as np
+
 import oracle
 
 GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "rng_golden.json")))
@@ -54,3 +56,27 @@ def test_discrete_distribution_and_draw_count():
         assert got == e["idx"]
         # the next canonical shows how many outputs the samples consumed
         assert LIB.oracle_canonical(C.byref(s)) == float.fromhex(e["next"])
+
+
+def test_default_stream_and_shuffle():
+    """settings::rng starts from a default-constructed pcg32; std::shuffle
+    over it (the branchless power iteration's combing) draws its swap
+    positions by libstdc++'s two paths: the oracle's restatement gives the
+    same permutations and leaves the stream in the same state."""
+    g = GOLD
+    st = C.c_uint64(0)
+    oracle.load().oracle_pcg32_seed(0xcafef00dd15ea5e5, C.byref(st))
+    assert st.value == g["default_state"]
+    lib = oracle.load()
+    for case in g["shuffle"]:
+        n = case["n"]
+        v = np.arange(n, dtype=np.uint32)
+        s = C.c_uint64(0)
+        lib.oracle_pcg32_seed(case["seed"], C.byref(s))
+        lib.oracle_shuffle(v.ctypes.data, n, 4, C.byref(s))
+        check = 0
+        for x in v.tolist():
+            check = (check * 1000003 + x) & ((1 << 64) - 1)
+        assert check == case["check"], n
+        assert v[:12].tolist() == case["head"], n
+        assert lib.oracle_pcg32_next(C.byref(s)) == case["next"], n
