@@ -290,7 +290,8 @@ def from_reference_deck(deck, nparticles=None, precision="fp64", tracking=None):
                        global_rng_skip=6 * (len(deck["cells"]) + sum(
                            1 for m in deck["materials"]
                            if not (isinstance(m.get("color"), list) and len(m["color"]) == 3))))
-    if st.get("regional-cancellation", False):
+    if st.get("cancellation", False):
+        # settings::regional_cancellation (src/parser.cpp:805-813)
         raise ValueError("regional cancellation is outside the multigroup transport path")
     for m in deck["materials"]:
         leg = {l: m[f"P{l}"] for l in range(1, 6) if f"P{l}" in m}
