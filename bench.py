@@ -129,6 +129,23 @@ def combine_replicas(dist, seconds, collisions, device):
     return float(tmax[0]), float(t[1])
 
 
+def host_cpu():
+    """The host's CPU, for the baseline lines: architecture and, where
+    /proc/cpuinfo names it, the model or the Arm part number."""
+    import platform
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                if k.strip() in ("model name", "CPU part") and v.strip():
+                    model = v.strip()
+                    break
+    except OSError:
+        pass
+    return f"{platform.machine()}" + (f" ({model})" if model else "")
+
+
 def cpu_baseline(config, nhist, precision_label="fp64"):
     """The oracle (CPU restatement of the reference, FP64) on all host cores, one
     bounded transport sample of the same workload."""
@@ -161,8 +178,9 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.config], "deck": args.config, "histories_per_step": args.ref_sample,
-                   "tracking": "delta", "precision": "fp64"},
-        "cpu_baseline": {"value": value, "unit": "collisions/s", "cores": cores, "kind": "port",
+                   "tracking": __import__("abeille_gb300.decks", fromlist=["CONFIGS"]).CONFIGS[args.config](
+                       nparticles=1).tracking, "precision": "fp64"},
+        "cpu_baseline": {"value": value, "unit": "collisions/s", "cores": cores, "kind": "port", "cpu": host_cpu(),
                          "sample": f"{args.ref_sample} first-generation histories of config {args.config} per step"},
         "e2e": {"value": value, "unit": "collisions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -295,7 +313,7 @@ def main():
     cpu = None
     if world == 1 and not args.no_cpu:
         v, cores, c, dt = cpu_baseline(args.config, args.cpu_sample)
-        cpu = {"value": v, "unit": "collisions/s", "cores": cores, "kind": "port",
+        cpu = {"value": v, "unit": "collisions/s", "cores": cores, "kind": "port", "cpu": host_cpu(),
                "sample": f"{args.cpu_sample} first-generation histories of config {args.config}, FP64, one transport"}
     line = {
         "metric": "collisions/s", "value": value, "unit": "collisions/s", "n_gpus": world, "steps": args.steps,
@@ -311,6 +329,7 @@ def main():
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": KERNELS_PER_GEN * args.steps,
         "clocks": clk.summary(),
+        "flights_per_s": flights / (step_ms / 1e3) * world,
         "detail": {"flights": flights, "collisions": coll, "sites": sites, "transport_ms": tr_ms,
                    "wall_s": wall, "kcol_last": recs[-1]["kcol"], "lost": sum(r["lost"] for r in recs)},
     }
@@ -410,6 +429,7 @@ def bench_batch(args):
             if secs_cpu > 15.0:
                 break
         cpu = {"value": c_sum / secs_cpu, "unit": "collisions/s", "cores": oracle.cores(), "kind": "port",
+               "cpu": host_cpu(),
                "sample": f"{used} of the problems, {nb} batches each, FP64, one problem at a time"}
     line = {
         "metric": "collisions/s", "value": coll_all / secs, "unit": "collisions/s", "n_gpus": world,
