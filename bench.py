@@ -662,9 +662,10 @@ def bench_server(args):
 
 
 # DRAM bytes (read + write) per history of a transport launch, from the ncu
-# capture in profiles/transport_kernel_config1_mixed_300k.md (157.6 MB at
-# 300,000 histories); bank, site and spill traffic grow with the histories.
-TRAFFIC_PER_HISTORY = {(1, "mixed"): 157.60e6 / 3e5}
+# captures in profiles/transport_kernel_config1_mixed_300k.md (157.6 MB at
+# 300,000 histories) and profiles/transport_kernel_config2_mixed_300k.md
+# (35.3 MB at 300,000); bank, site and spill traffic grow with the histories.
+TRAFFIC_PER_HISTORY = {(1, "mixed"): 157.60e6 / 3e5, (2, "mixed"): 35.30e6 / 3e5}
 L2_FLUSH_BYTES = 256 << 20
 
 if __name__ == "__main__":
