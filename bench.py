@@ -305,7 +305,7 @@ def main():
     achieved = alg / (tr_ms / 1e3) / 1e9
     peak, src = peaks()
     hist = sum(r["histories"] for r in recs) / max(len(recs), 1)
-    tph = TRAFFIC_PER_HISTORY.get((args.config, args.precision))
+    tph = TRAFFIC_PER_HISTORY.get((args.config, args.precision, builder.tracking))
     traffic = tph * hist if tph else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "peak_source": src,
@@ -665,7 +665,8 @@ def bench_server(args):
 # captures in profiles/transport_kernel_config1_mixed_300k.md (157.6 MB at
 # 300,000 histories) and profiles/transport_kernel_config2_mixed_300k.md
 # (35.3 MB at 300,000); bank, site and spill traffic grow with the histories.
-TRAFFIC_PER_HISTORY = {(1, "mixed"): 157.60e6 / 3e5, (2, "mixed"): 35.30e6 / 3e5}
+TRAFFIC_PER_HISTORY = {(1, "mixed", "delta-tracking"): 157.60e6 / 3e5,
+                       (2, "mixed", "surface-tracking"): 35.30e6 / 3e5}
 L2_FLUSH_BYTES = 256 << 20
 
 if __name__ == "__main__":
