@@ -108,3 +108,22 @@ def test_run_a_reference_deck_from_yaml():
     st = run_deck(text, precision="mixed", particles=100000, generations=40, ignored=10, is_text=True, out=buf)
     assert abs(st["kcol_avg"] - ref["_expected_k"]) < 4 * st["kcol_std"] + 2e-4, buf.getvalue()
     assert "k_col" in buf.getvalue()
+
+
+def test_branchless_settings_round_trip():
+    """A branchless-k-eigenvalue deck keeps its collision flags through the
+    writer and the reader, and the global stream's skip counts the deck's
+    cells and materials (6 outputs each for their plot colours)."""
+    b = decks.config0(nparticles=100)
+    b.mode = "branchless-k-eigenvalue"
+    b.branchless_material, b.branchless_splitting, b.branchless_combing = False, True, True
+    text = deck.dump_yaml(b.to_deck(ngenerations=5, nignored=1))
+    b2, d = deck.deck_from_text(text)
+    assert d["settings"]["simulation"] == "branchless-k-eigenvalue"
+    assert (b2.branchless_material, b2.branchless_splitting, b2.branchless_combing) == (False, True, True)
+    s1, s2 = b.build(precision="fp64").struct.settings, b2.build(precision="fp64").struct.settings
+    assert s1.branchless == s2.branchless == 1 | 4 | 8
+    assert s2.global_rng_skip == 6 * (len(d["cells"]) + len(d["materials"])) == s1.global_rng_skip
+    d["settings"]["cancellation"] = True
+    with pytest.raises(ValueError):
+        deck.deck_from_text(deck.dump_yaml(d))
