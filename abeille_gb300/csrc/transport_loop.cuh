@@ -141,9 +141,10 @@ ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& ac
   }
 }
 
-// Occupancy (measured on config 1 and config 2): FP32 delta tracking (and
-// implicit-leakage delta tracking) runs four 256-thread blocks per SM (64
-// registers), FP32 surface tracking three (80 registers), FP64 three (80).
+// Occupancy (measured on the 51x51-pin assembly and the 70-group
+// nested-cylinder lattice): FP32 delta tracking (and implicit-leakage delta
+// tracking) runs four 256-thread blocks per SM (64 registers), FP32 surface
+// tracking three (80 registers), FP64 three (80).
 // TRACK: the tracking mode, or'd with ABX_KERNEL_BRANCHLESS for the
 // branchless collisions of the branchless k-eigenvalue simulation.
 template <class R, int TRACK, bool ISO>
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
   constexpr bool BL = (TRACK & ABX_KERNEL_BRANCHLESS) != 0;
   // Event traces are a parity-test hook of the FP64 mode (abx_set_trace
   // refuses mixed contexts): the FP32 kernels carry none of their code
-  // (config 2 +5 %, config 1 within noise).
+  // (the nested-cylinder lattice +5 %, the pin assembly within noise).
   const bool TRACE = sizeof(R) == 8 && A.trace != nullptr;
   const Tables& T = A.T;
   const View<R> V = make_view<R>(T);
