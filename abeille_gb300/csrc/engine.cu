@@ -1233,9 +1233,11 @@ static int check_state(abx_ctx* c) {
   return ABX_OK;
 }
 
-// which transport kernel: the tracking mode, plus the branchless-collision bit
+// which transport kernel: the tracking mode, plus the branchless-collision
+// bit, plus the single-problem bit outside runs that score per problem
 static int kernel_code(const abx_ctx* c) {
-  return c->prob0.tracking | (c->prob0.branchless ? ABX_KERNEL_BRANCHLESS : 0);
+  return c->prob0.tracking | (c->prob0.branchless ? ABX_KERNEL_BRANCHLESS : 0) |
+         (c->batch_scores ? 0 : ABX_KERNEL_SINGLE);
 }
 
 template <class R> static TransportArgs<R> make_args(abx_ctx* c, const BankT<R>& bank, const SiteT<R>& sites,

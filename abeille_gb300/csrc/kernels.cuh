@@ -52,9 +52,11 @@ template <class R> struct TransportArgs {
 };
 
 enum : int { ABX_PSCORES = 5, ABX_PCOUNTS = 4 };
-// transport kernel codes: the tracking mode (ABX_TRACK_*) or'd with this bit
-// for branchless collisions
-enum : int { ABX_KERNEL_BRANCHLESS = 0x100 };  // counters: collisions flights histories lost
+// transport kernel codes: the tracking mode (ABX_TRACK_*) or'd with these
+// bits: branchless collisions; one problem without per-problem scores (every
+// history of the launch belongs to problem 0, the batch bookkeeping compiled
+// out)
+enum : int { ABX_KERNEL_BRANCHLESS = 0x100, ABX_KERNEL_SINGLE = 0x200 };  // counters: collisions flights histories lost
 
 template <class R> ABX_DEV View<R> make_view(const Tables& T);
 template <> ABX_DEV View<double> make_view<double>(const Tables& T) {

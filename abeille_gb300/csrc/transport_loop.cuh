@@ -34,7 +34,7 @@ enum : int {
 
 // Load history h into a lane (DeltaTracker::transport, src/delta_tracker.cpp:87-103);
 // its location is found by the next descend phase.
-template <class R>
+template <class R, bool SINGLE>
 ABX_DEV bool lane_load(const TransportArgs<R>& A, const Tables& T, const View<R>& V, Lane<R>& L, Trk<R>& k,
                        uint32_t h) {
   L.h = h;
@@ -44,13 +44,13 @@ ABX_DEV bool lane_load(const TransportArgs<R>& A, const Tables& T, const View<R>
   L.w = A.bank.w[h];
   L.w2 = A.bank.w2 ? A.bank.w2[h] : R(0);
   L.rng = A.bank.rng[h];
-  L.pid = A.bank.prob ? A.bank.prob[h] : 0;
+  L.pid = (!SINGLE && A.bank.prob) ? A.bank.prob[h] : 0;
   L.rb = L.r;
   L.dau = 0;
   L.nsec = 0;
   L.events = 0;
   L.hcoll = 0;
-  const ProbT& P = T.probs[L.pid];
+  const ProbT& P = T.probs[SINGLE ? 0 : L.pid];
   L.g = group_of<R>(V.ebnd + P.eb_off, P.G, L.E);
   k.r = L.r;
   k.u = L.u;
@@ -127,10 +127,10 @@ ABX_DEV void carter_split(const TransportArgs<R>& A, const ProbT& P, Lane<R>& L)
 // End of a history: its fission-site count (for the bank sort) and its score
 // totals, to the block's accumulators or, in a batch of problems, to its
 // problem's sums and counters.
-template <class R>
+template <class R, bool SINGLE>
 ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& acc, double* sh_acc) {
   A.hist_count[L.h] = L.dau;
-  if (A.pscore) {
+  if (!SINGLE && A.pscore) {
     acc.flush(A.pscore + (size_t)L.pid * ABX_PSCORES);
     unsigned long long* c = A.pcount + (size_t)L.pid * ABX_PCOUNTS;
     atomicAdd(c + 0, (unsigned long long)L.hcoll);
@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
     transport_kernel(const __grid_constant__ TransportArgs<R> A) {
   constexpr int TRK = TRACK & 0xff;
   constexpr bool BL = (TRACK & ABX_KERNEL_BRANCHLESS) != 0;
+  constexpr bool SINGLE = (TRACK & ABX_KERNEL_SINGLE) != 0;
   // Event traces are a parity-test hook of the FP64 mode (abx_set_trace
   // refuses mixed contexts): the FP32 kernels carry none of their code
   // (the nested-cylinder lattice +5 %, the pin assembly within noise).
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
 #define ABX_LOST()                                                                              \
   {                                                                                             \
     nlost++;                                                                                    \
-    if (A.pcount) atomicAdd(A.pcount + (size_t)L.pid * ABX_PCOUNTS + 3, 1ull);                  \
+    if (!SINGLE && A.pcount) atomicAdd(A.pcount + (size_t)L.pid * ABX_PCOUNTS + 3, 1ull);       \
     if (TRACE) trace_rec(A, L, 7, k.cell);                                                      \
   }
 
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
         if (h >= n_hist || st->err) {
           done = true;
           ph = PH_DONE;
-        } else if (!lane_load(A, T, V, L, k, (uint32_t)h)) {
+        } else if (!lane_load<R, SINGLE>(A, T, V, L, k, (uint32_t)h)) {
           ABX_FAIL(k.err);
         } else {
           dmode = 1;
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
 
     // ---------------------------------------------------------------- flight
     if (ph == PH_FLIGHT) {
-      const ProbT& P = T.probs[L.pid];
+      const ProbT& P = T.probs[SINGLE ? 0 : L.pid];
       L.events++;
       nflight++;
       if (TRK == ABX_TRACK_IMPLICIT_LEAKAGE) {
@@ -360,7 +361,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
       // CellUniverse/RectLattice::get_cell: re-descent from the first invalid
       // pad, or from the root (restart_get_current) when that fails or when the
       // tree must be rebuilt.
-      const ProbT& P = T.probs[L.pid];
+      const ProbT& P = T.probs[SINGLE ? 0 : L.pid];
       int cell = -1;
       if (dmode == 2) {
         cell = univ_get_cell(T, V, k, dui, dfr, k.getfr(dfr));
@@ -381,7 +382,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
     if (ph == PH_START) {
       if (k.cell < 0) {  // lost at birth: a warning in the reference, the particle is killed
         ABX_LOST();
-        history_end(A, L, acc, sh_acc);
+        history_end<R, SINGLE>(A, L, acc, sh_acc);
         ph = PH_REFILL;
       } else {
         L.mat = T.cells[k.cell].fill;
@@ -448,7 +449,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
           ph = PH_DEAD;
         }
       } else {
-        const ProbT& P = T.probs[L.pid];
+        const ProbT& P = T.probs[SINGLE ? 0 : L.pid];
         if (TRK != ABX_TRACK_IMPLICIT_LEAKAGE && converged && P.has_tle) score_flight(T, V, P, L, dcol);
         L.r = add(L.r, scl(L.u, dcol));
         L.mat = T.cells[k.cell].fill;
@@ -488,7 +489,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
 
     // -------------------------------------------------------------- boundary
     if (ph == PH_LOST) {
-      const ProbT& P = T.probs[L.pid];
+      const ProbT& P = T.probs[SINGLE ? 0 : L.pid];
       const Bound<R> b = trk_bc_ool<R>(T, P, k);
       if (converged && P.has_tle) score_flight(T, V, P, L, dcol < b.dist ? dcol : b.dist);
       if (b.btype == ABX_BC_VACUUM) {
@@ -513,7 +514,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
     // --------------------------------------------------------------- collide
     __syncwarp();
     if (ph == PH_COLL) {
-      const ProbT& P = T.probs[L.pid];
+      const ProbT& P = T.probs[SINGLE ? 0 : L.pid];
       bool alive = true;
       ncoll++;
       L.hcoll++;
@@ -534,7 +535,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
     if (ph == PH_DEAD) {
       if (L.nsec > 0) {
         // Particle::resurect (include/simulation/particle.hpp:170-182)
-        const ProbT& P = T.probs[L.pid];
+        const ProbT& P = T.probs[SINGLE ? 0 : L.pid];
         L.nsec--;
         const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
         const R* sp = A.sec + ((uint64_t)gt * A.sec_cap + L.nsec) * 9;
@@ -552,7 +553,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
           ph = PH_WAIT;
         }
       } else {
-        history_end(A, L, acc, sh_acc);
+        history_end<R, SINGLE>(A, L, acc, sh_acc);
         ph = PH_REFILL;
       }
     }
@@ -562,7 +563,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
         // mixed mode: a history this long is a geometry rounding trap, not
         // physics; it is counted in `lost` and ended
         ABX_LOST();
-        history_end(A, L, acc, sh_acc);
+        history_end<R, SINGLE>(A, L, acc, sh_acc);
         ph = PH_REFILL;
       } else {
         ABX_FAIL(ABX_ERR_TIMEOUT);

@@ -11,9 +11,20 @@ namespace abx {
 
 template __global__ void transport_kernel<float, ABX_TRACK_DELTA, false>(const __grid_constant__ TransportArgs<float>);
 template __global__ void transport_kernel<float, ABX_TRACK_DELTA, true>(const __grid_constant__ TransportArgs<float>);
+// one problem, no per-problem bookkeeping (the power iteration, transport
+// steps and fixed-source runs of a single problem)
+constexpr int DELTA_SINGLE = ABX_TRACK_DELTA | ABX_KERNEL_SINGLE;
+template __global__ void transport_kernel<float, DELTA_SINGLE, false>(const __grid_constant__ TransportArgs<float>);
+template __global__ void transport_kernel<float, DELTA_SINGLE, true>(const __grid_constant__ TransportArgs<float>);
 
 void launch_transport_f(const TransportArgs<float>& A, int tracking, bool iso, bool trace, int grid, int block,
                         cudaStream_t s) {
+  if (tracking == DELTA_SINGLE) {
+    if (iso) transport_kernel<float, DELTA_SINGLE, true><<<grid, block, 0, s>>>(A);
+    else transport_kernel<float, DELTA_SINGLE, false><<<grid, block, 0, s>>>(A);
+    return;
+  }
+  tracking &= ~ABX_KERNEL_SINGLE;  // the other kernels serve single problems too
   if (tracking & ABX_KERNEL_BRANCHLESS) {
     launch_transport_f_branchless(A, tracking & 0xff, iso, grid, block, s);
   } else if (tracking == ABX_TRACK_SURFACE) {
@@ -28,6 +39,13 @@ void launch_transport_f(const TransportArgs<float>& A, int tracking, bool iso, b
 }
 
 int occupancy_f(int tracking, bool iso, int block) {
+  if (tracking == DELTA_SINGLE) {
+    int nb = 0;
+    if (iso) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<float, DELTA_SINGLE, true>, block, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, transport_kernel<float, DELTA_SINGLE, false>, block, 0);
+    return nb;
+  }
+  tracking &= ~ABX_KERNEL_SINGLE;
   if (tracking & ABX_KERNEL_BRANCHLESS) return occupancy_f_branchless(tracking & 0xff, iso, block);
   if (tracking == ABX_TRACK_SURFACE) return occupancy_f_surface(iso, block);
   if (tracking == ABX_TRACK_IMPLICIT_LEAKAGE || tracking == ABX_TRACK_CARTER)
