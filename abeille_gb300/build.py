@@ -1,6 +1,6 @@
 """In-tree build of the CUDA engine (sm_103a) into abeille_gb300/_lib/.
 
-Seven translation units are compiled in parallel with nvcc and linked into one
+Eight translation units are compiled in parallel with nvcc and linked into one
 shared library exposing the C-ABI of include/abeille_gb300.h:
 
   engine.cu                   host side + bookkeeping kernels     --fmad=false
@@ -8,6 +8,8 @@ shared library exposing the C-ABI of include/abeille_gb300.h:
   transport_mixed.cu          FP32-tracking kernels, delta tracking
   transport_mixed_surface.cu  FP32-tracking kernels, surface tracking
   transport_mixed_variants.cu FP32-tracking kernels, implicit-leakage and Carter tracking
+  transport_mixed_branchless.cu FP32-tracking kernels, branchless collisions
+  problem_tables.cpp          host table derivation (problems appended to the pools)
   server.cpp                  request loop (host scheduler thread)
 
 Host code is compiled with -ffp-contract=off so derived tables round the same
@@ -35,6 +37,7 @@ UNITS = [
     ("transport_mixed_surface.cu", []),
     ("transport_mixed_variants.cu", []),
     ("transport_mixed_branchless.cu", []),
+    ("problem_tables.cpp", []),
     ("server.cpp", []),
 ]
 
