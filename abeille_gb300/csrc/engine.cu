@@ -1,9 +1,10 @@
 // Host side of the GB300 multigroup transport engine: the C-ABI declared in
-// include/abeille_gb300.h, table derivation, device pools, and the
-// device-resident generation loop (bank sort, weight normalisation, entropy,
-// k and tally statistics) that replaces the reference's PowerIterator /
-// FixedSource bookkeeping.  Compiled with --fmad=false and host
-// -ffp-contract=off: every double derived here rounds as the reference's does.
+// include/abeille_gb300.h, device pools (the tables come from
+// problem_tables.cpp), and the device-resident generation loop (bank sort,
+// weight normalisation, entropy, k and tally statistics) that replaces the
+// reference's PowerIterator / FixedSource bookkeeping.  Compiled with
+// --fmad=false and host -ffp-contract=off: every double derived here rounds
+// as the reference's does.
 #include <cuda_runtime.h>
 
 #include <algorithm>
