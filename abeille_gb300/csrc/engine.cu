@@ -680,11 +680,13 @@ template <class R> __global__ void k_bank_to_aos(BankT<R> b, size_t n, abx_parti
     out[i] = p;
   }
 }
-// Sorted sites -> AoS BankedParticles.
+// Sorted sites -> AoS BankedParticles.  `cap` bounds both the site arrays
+// and `out`: the transport kernel counts sites past its capacity without
+// storing them, so entries at or beyond `cap` were never written.
 template <class R>
 __global__ void k_sites_to_aos(SiteT<R> S, const DevState* st, const uint32_t* off, BankT<R> cur, abx_site* out,
                                uint64_t cap) {
-  const unsigned long long ns = st->site_count;
+  const unsigned long long ns = st->site_count < cap ? st->site_count : (unsigned long long)cap;
   for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < ns;
        j += (unsigned long long)gridDim.x * blockDim.x) {
     uint32_t h = S.hist[j];
@@ -991,6 +993,8 @@ extern "C" int abx_transport(abx_ctx* c, const abx_particle* bank, size_t n, dou
   if (!c || (!bank && n)) return fail(ABX_ERR_INVALID, "bad arguments");
   if (!(kcol > 0)) return fail(ABX_ERR_INVALID, "kcol must be positive");
   if (n > 0xffffffffull) return fail(ABX_ERR_INVALID, "at most 2^32-1 histories per call");
+  if (c->nprob > 1)
+    return fail(ABX_ERR_UNSUPPORTED, "a batch context transports through abx_run_fixed_source_batch only");
   cudaSetDevice(c->device);
   const bool mixed = mixed_of(c);
   const bool keig = c->prob0.mode == ABX_MODE_K_EIGENVALUE;
@@ -1218,6 +1222,8 @@ extern "C" int abx_transport_noalloc(abx_ctx* c, const abx_particle* bank_dev, s
                                      abx_site* sites_dev, size_t site_capacity, size_t* n_sites, abx_scores* scores) {
   if (!c || (!bank_dev && n)) return fail(ABX_ERR_INVALID, "bad arguments");
   if (!(kcol > 0)) return fail(ABX_ERR_INVALID, "kcol must be positive");
+  if (c->nprob > 1)
+    return fail(ABX_ERR_UNSUPPORTED, "a batch context transports through abx_run_fixed_source_batch only");
   if (n > NA_HIST)
     return fail(ABX_ERR_CAPACITY, "abx_transport_noalloc takes at most %zu histories per call (got %zu)", NA_HIST, n);
   if (site_capacity > NA_SITES)

@@ -335,7 +335,8 @@ int abx_sample_sources(abx_ctx* ctx, uint64_t first_history_id, size_t n,
  * `converged` is settings::converged (mesh tallies score only when set).
  * Sites come back in BankedParticle::operator< order, i.e. the order the
  * reference concatenates per-history banks.  In fixed-source mode fission
- * produces in-history secondaries and *n_sites is 0. */
+ * produces in-history secondaries and *n_sites is 0.  A batch context
+ * (abx_create_batch) returns ABX_ERR_UNSUPPORTED. */
 int abx_transport(abx_ctx* ctx, const abx_particle* bank, size_t n, double kcol,
                   int converged, abx_site* sites, size_t site_capacity,
                   size_t* n_sites, abx_scores* scores);
@@ -348,8 +349,11 @@ int abx_transport(abx_ctx* ctx, const abx_particle* bank, size_t n, double kcol,
  * `bank_dev` and `sites_dev` are device buffers the caller owns (layouts as
  * abx_particle / abx_site); *n_sites and *scores come back on the host.
  * Limits: at most 16384 histories and 65536 fission sites per call (larger
- * requests return ABX_ERR_CAPACITY); fixed-source problems with fissile
- * materials are refused (their secondaries need abx_transport).
+ * requests return ABX_ERR_CAPACITY, as does a fission bank that outgrows
+ * `site_capacity`).  ABX_ERR_UNSUPPORTED, because their particles go on
+ * per-thread stacks this entry point does not hold: fixed-source problems
+ * with fissile materials (in-history secondaries), Carter tracking and
+ * branchless collisions with splitting; also batch contexts.
  * All per-call scratch is one fixed 6 MB device array, reserved on every GPU
  * that loads the library and held until the process exits.  Every call uses
  * that same array, so calls that overlap on the GPU race.  The first call on
