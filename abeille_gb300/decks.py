@@ -20,6 +20,11 @@ bounded by the boundary-condition surfaces.
            groups, P1 scattering with mean cosine in [0, 0.3]; 100 cm tall,
            vacuum top/bottom; 100x100x50 track-length flux tally.
   config3  non-multiplying fixed-source slab boxes (see fixed_source_problem).
+  quadrics every other surface kind of the path in one cell universe: a fuel
+           sphere, a fuel x-cylinder rod, a water y-cylinder rod, moderator
+           split by a general plane, inside a vacuum sphere cut by a
+           reflective general plane; 7 groups; collision and track-length
+           flux tallies.
 """
 import numpy as np
 
@@ -188,6 +193,39 @@ def seventy_group_xs(seed=1, nfuel=8):
     mats.append(base(0.6, 0.8, 0.05, False))   # clad
     mats.append(base(0.95, 0.97, 0.15, False))  # moderator
     return mats
+
+
+def quadrics(nparticles=4096, precision="fp64", tracking="delta-tracking", legendre=False):
+    """Spheres, general planes (normals off the axes, one of them a reflective
+    boundary) and x/y-cylinders, the surface kinds the lattice configurations
+    do not use (src/sphere.cpp, src/plane.cpp, src/xcylinder.cpp,
+    src/ycylinder.cpp).  With `legendre`, the moderator scatters with a P1
+    moment (mean cosine 0.2), so angle tables are sampled as well."""
+    fuel, mod, water = seven_group_xs()
+    b = ProblemBuilder(7, np.arange(8.0), nparticles=nparticles, precision=precision, tracking=tracking)
+    b.material(1, **fuel)
+    if legendre:
+        mod = dict(mod, legendre={1: 0.2 * np.asarray(mod["scatter"])})
+    b.material(2, **mod)
+    b.material(3, **water)
+    b.surface("sphere", 1, x0=0.0, y0=0.0, z0=0.0, r=3.0)
+    b.surface("xcylinder", 2, y0=6.0, z0=3.0, r=1.5)
+    b.surface("ycylinder", 3, x0=-6.0, z0=-3.0, r=1.5)
+    b.surface("plane", 4, A=0.6, B=0.48, C=0.64, D=1.5)
+    b.surface("sphere", 5, x0=0.0, y0=0.0, z0=0.0, r=11.0, boundary="vacuum")
+    b.surface("plane", 6, A=0.3, B=-0.4, C=0.8660254037844386, D=5.0, boundary="reflective")
+    b.cell(1, "-1", material=1)
+    b.cell(2, "-2 & -5 & -6", material=1)
+    b.cell(3, "-3 & -5 & -6", material=3)
+    b.cell(4, "+1 & +2 & +3 & -4 & -5 & -6", material=2)
+    b.cell(5, "+1 & +2 & +3 & +4 & -5 & -6", material=3)
+    b.cell_universe(1, [1, 2, 3, 4, 5])
+    b.set_root(1)
+    b.mesh_tally([11, 11, 11], [-11.0, -11.0, -11.0], [11.0, 11.0, 11.0], "collision", "flux", [0.0, 7.0])
+    b.mesh_tally([11, 11, 11], [-11.0, -11.0, -11.0], [11.0, 11.0, 11.0], "track-length", "flux", [0.0, 7.0])
+    b.set_entropy([-11.0, -11.0, -11.0], [11.0, 11.0, 11.0], [8, 8, 8])
+    b.source("box", low=[-3.0, -3.0, -3.0], hi=[3.0, 3.0, 3.0], energy=0.5, fissile_only=True)
+    return b
 
 
 def config2(nparticles=2000000, precision="fp64", tracking="surface-tracking"):

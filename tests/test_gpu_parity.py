@@ -68,6 +68,29 @@ def test_event_traces_match_per_history(cfg, tracking):
     compare_traces(eng.get_trace(), ora.get_trace())
 
 
+def test_c5g7_transport_step_matches():
+    """The reference's C5G7 core (input_files/c5g7.yaml: 2x2 assemblies of
+    17x17 pins, seven materials, delta tracking, track-length tally): fission
+    bank, scores and tally of one transport step against the oracle."""
+    b = decks.from_reference_deck(reference_deck("c5g7"), nparticles=4096)
+    eng, ora, _ = pair(b, nthreads=oracle.cores())
+    bank = ora.sample_sources(0, 4096)
+    sg, cg = eng.transport(bank, 1.1, True)
+    sc, cc = ora.transport(bank, 1.1, True)
+    assert len(sg) == len(sc) > 0
+    assert np.array_equal(sg["parent_history_id"], sc["parent_history_id"])
+    assert np.array_equal(sg["parent_daughter_id"], sc["parent_daughter_id"])
+    assert close(sg["r"], sc["r"], atol=1e-9) and close(sg["u"], sc["u"], atol=1e-9)
+    for k in ("collisions", "flights", "lost"):
+        assert cg[k] == cc[k], k
+    for k in ("k_col", "k_abs", "leakage", "mig_area"):
+        assert abs(cg[k] - cc[k]) <= RTOL * abs(cc[k]) + 1e-300, (k, cg[k], cc[k])
+    tg, tc = eng.tally(0)["gen"], ora.tally(0)["gen"]
+    assert np.array_equal(tg != 0, tc != 0) and abs(tg.sum() - tc.sum()) <= RTOL * tc.sum()
+    assert close(tg, tc, rtol=1e-9, atol=0.0)
+    eng.close()
+
+
 @pytest.mark.parametrize("cfg,tracking", [(0, "delta-tracking"), (1, "delta-tracking"), (2, "surface-tracking"),
                                           (2, "delta-tracking"), (1, "implicit-leakage-delta-tracking"),
                                           (2, "implicit-leakage-delta-tracking")])
@@ -189,9 +212,22 @@ def test_fixed_source_matches():
     assert np.allclose(eng.tally(0)["avg"], ora.tally(0)["avg"], rtol=1e-10, atol=0)
 
 
-@pytest.mark.parametrize("name", ["PUa-1-0-IN", "PUb-1-0-SL", "Ua-1-1-CY"])
-def test_reference_decks_trace_parity(name):
-    b = decks.from_reference_deck(DECKS[name], nparticles=256)
+def reference_deck(name):
+    """A reference deck from the fixtures; c5g7's 1224x1224x10 track-length
+    tally is cut to 51x51x10 bins over the same extent (parity tests need the
+    estimator, not the resolution)."""
+    d = dict(DECKS[name])
+    if name == "c5g7":
+        d["tallies"] = [dict(t, shape=[51, 51, 10]) for t in d["tallies"]]
+    return d
+
+
+@pytest.mark.parametrize("name,tracking", [("PUa-1-0-IN", None), ("PUb-1-0-SL", None), ("Ua-1-1-CY", None),
+                                           ("PUa-1-1-SL", None), ("PUa-1-2-SL", None), ("Ua-1-1-IN", None),
+                                           ("PUa-1-2-SL", "delta-tracking"), ("c5g7", "delta-tracking"),
+                                           ("c5g7", "surface-tracking")])
+def test_reference_decks_trace_parity(name, tracking):
+    b = decks.from_reference_deck(reference_deck(name), nparticles=256, tracking=tracking)
     eng, ora, _ = pair(b)
     bank = ora.sample_sources(0, 256)
     eng.set_trace(128, 1 << 20)
