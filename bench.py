@@ -230,6 +230,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=200000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run of the mixed mode")
     ap.add_argument("--tracking", default=None,
                     choices=["delta-tracking", "surface-tracking", "implicit-leakage-delta-tracking", "carter-tracking"])
     ap.add_argument("--problems", type=int, default=4096, help="config 3: problems in the batch")
@@ -296,6 +297,25 @@ def main():
         v, h2d, d2h = e2e_measure(eng, bank, kcol, max(2, args.steps // 3), 1)
         e2e = {"value": v * world, "unit": "collisions/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
+    fp64 = None
+    if args.precision == "mixed" and not args.no_fp64 and world == 1:
+        # the plain FP64 GPU path on the same deck and history count, device
+        # time per generation as above: the mixed/FP64 ratio of the same run
+        eng.close()
+        fb = decks.CONFIGS[args.config](nparticles=npart)
+        if args.tracking:
+            fb.tracking = args.tracking
+        eng64 = Engine(fb.build(precision="fp64"), local)
+        _abi.check(eng64.lib.abx_set_l2_flush(eng64.ctx, L2_FLUSH_BYTES), eng64.lib)
+        eng64.run_power_iteration(max(args.warmup, 1), 0)
+        n64 = max(3, args.steps // 4)
+        _, r64 = eng64.run_power_iteration_records(n64, 0)
+        c64 = sum(r["collisions"] for r in r64)
+        ms64 = sum(r["step_ms"] for r in r64)
+        fp64 = {"value": c64 / (ms64 / 1e3), "unit": "collisions/s", "generations": n64,
+                "ms_per_step": ms64 / n64}
+        eng64.close()
+
     if rank != 0:
         if dist:
             dist.barrier()
@@ -331,7 +351,8 @@ def main():
         "clocks": clk.summary(),
         "flights_per_s": flights / (step_ms / 1e3) * world,
         "detail": {"flights": flights, "collisions": coll, "sites": sites, "transport_ms": tr_ms,
-                   "wall_s": wall, "kcol_last": recs[-1]["kcol"], "lost": sum(r["lost"] for r in recs)},
+                   "wall_s": wall, "kcol_last": recs[-1]["kcol"], "lost": sum(r["lost"] for r in recs),
+                   "fp64": fp64, "mixed_over_fp64": (value / fp64["value"]) if fp64 else None},
     }
     print(json.dumps(line), flush=True)
     if dist:
