@@ -195,6 +195,8 @@ PROTOTYPES = {
     "abx_last_transport_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "abx_set_l2_flush": (C.c_int, [C.c_void_p, C.c_size_t]),
     "abx_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
+    "abx_set_transport_kernel": (C.c_int, [C.c_void_p, C.c_int]),
+    "abx_get_transport_kernel": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "abx_autotune": (C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                C.POINTER(C.c_double)]),
     "abx_create_batch": (C.c_int, [C.POINTER(Problem), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),

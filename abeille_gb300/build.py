@@ -1,6 +1,6 @@
 """In-tree build of the CUDA engine (sm_103a) into abeille_gb300/_lib/.
 
-Eight translation units are compiled in parallel with nvcc and linked into one
+Ten translation units are compiled in parallel with nvcc and linked into one
 shared library exposing the C-ABI of include/abeille_gb300.h:
 
   engine.cu                   host side + bookkeeping kernels     --fmad=false
@@ -9,6 +9,8 @@ shared library exposing the C-ABI of include/abeille_gb300.h:
   transport_mixed_surface.cu  FP32-tracking kernels, surface tracking
   transport_mixed_variants.cu FP32-tracking kernels, implicit-leakage and Carter tracking
   transport_mixed_branchless.cu FP32-tracking kernels, branchless collisions
+  transport_pool_mixed.cu     pooled (event-sorted) FP32-tracking kernels
+  transport_pool_fp64.cu      pooled FP64 parity kernels               --fmad=false
   problem_tables.cpp          host table derivation (problems appended to the pools)
   server.cpp                  request loop (host scheduler thread)
 
@@ -37,6 +39,8 @@ UNITS = [
     ("transport_mixed_surface.cu", []),
     ("transport_mixed_variants.cu", []),
     ("transport_mixed_branchless.cu", []),
+    ("transport_pool_mixed.cu", []),
+    ("transport_pool_fp64.cu", ["--fmad=false"]),
     ("problem_tables.cpp", []),
     ("server.cpp", []),
 ]

@@ -317,6 +317,11 @@ struct abx_context {
   int gen_nignored = -1;
   std::vector<const void*> gen_sig;  // buffers the captured launches point at
   std::vector<cudaEvent_t> ev_pool;  // per-generation timing events
+  // transport kernel choice (ABX_TRANSPORT_KERNEL_*) and the pooled kernel's
+  // slot records
+  int kernel_mode = ABX_TRANSPORT_KERNEL_AUTO;
+  void* pool = nullptr;
+  size_t pool_bytes = 0;
 };
 
 static void ctx_free(abx_ctx* c) {
@@ -328,6 +333,8 @@ static void ctx_free(abx_ctx* c) {
   for (auto& b : c->bf) b.free_();
   c->sd.free_();
   c->sf.free_();
+  if (c->pool) cudaFree(c->pool);
+  c->pool = nullptr;
   void* ps[] = {c->tally_gen, c->tally_avg, c->tally_var, c->st, c->run, c->gen_rec,
                 c->ent_bins, c->ent_total, c->hist_count, c->offsets, c->block_sums, c->sec,
                 c->aos_in, c->aos_out, c->trace, c->flush, c->pscore, c->pcount, c->prun,
@@ -742,7 +749,54 @@ static int ensure_sites(abx_ctx* c, size_t n, bool mixed) {
   return ABX_OK;
 }
 
+static int kernel_code(const abx_ctx* c);
+
+// Histories of this context can put particles on a secondary stack:
+// fission in fixed-source problems, splitting in Carter tracking and in
+// branchless collisions with splitting.
+static bool needs_stacks(const abx_ctx* c) {
+  const bool bl_split = (c->prob0.branchless & ABX_BRANCHLESS_SPLITTING) != 0;
+  return c->prob0.tracking == ABX_TRACK_CARTER || bl_split ||
+         (c->prob0.mode == ABX_MODE_FIXED_SOURCE && c->fissile_any);
+}
+
+// The pooled kernel serves delta and surface tracking with branching
+// collisions and no secondary stacks; everything else runs in the history
+// kernel.
+static bool pool_eligible(const abx_ctx* c) {
+  return (c->prob0.tracking == ABX_TRACK_DELTA || c->prob0.tracking == ABX_TRACK_SURFACE) && !c->prob0.branchless &&
+         !needs_stacks(c) && c->block <= 256;
+}
+static bool use_pool(const abx_ctx* c) {
+  if (c->kernel_mode == ABX_TRANSPORT_KERNEL_HISTORY || !pool_eligible(c)) return false;
+  if (c->kernel_mode == ABX_TRANSPORT_KERNEL_POOL) return true;
+  return false;  // automatic choice: the history kernel
+}
+static int occupancy_of(const abx_ctx* c, bool mixed, int block) {
+  if (use_pool(c)) return mixed ? occupancy_pool_f(kernel_code(c), c->all_iso, block) : occupancy_pool_d(kernel_code(c), block);
+  return mixed ? occupancy_f(kernel_code(c), c->all_iso, block) : occupancy_d(kernel_code(c), block);
+}
+static int ensure_pool(abx_ctx* c, bool mixed) {
+  if (!use_pool(c)) return ABX_OK;
+  const size_t warps = ((size_t)c->grid * c->block + 31) / 32;
+  const size_t need = warps * POOL_SLOTS_PER_WARP * (mixed ? pool_slot_bytes_f() : pool_slot_bytes_d());
+  if (c->pool && c->pool_bytes >= need) return ABX_OK;
+  if (c->pool) cudaFree(c->pool);
+  c->pool = nullptr;
+  c->pool_bytes = 0;
+  CUDA_TRY(cudaMalloc(&c->pool, need));
+  c->pool_bytes = need;
+  return ABX_OK;
+}
+
+static int ensure_stacks(abx_ctx* c, bool mixed);
 static int ensure_sec(abx_ctx* c, bool mixed) {
+  int rc = ensure_stacks(c, mixed);
+  if (rc != ABX_OK) return rc;
+  return ensure_pool(c, mixed);
+}
+
+static int ensure_stacks(abx_ctx* c, bool mixed) {
   // secondaries: fission in fixed-source problems, splitting in Carter tracking
   // splitting (Carter tracking, branchless collisions) needs the stack in
   // every mode
@@ -809,16 +863,21 @@ template <class R> static TransportArgs<R> make_args(abx_ctx* c, const BankT<R>&
   A.max_events = c->max_events;
   A.pscore = c->batch_scores ? c->pscore : nullptr;
   A.pcount = c->batch_scores ? c->pcount : nullptr;
+  A.pool = use_pool(c) ? c->pool : nullptr;
   return A;
 }
 
 static int launch_transport(abx_ctx* c, bool mixed, int which_bank, size_t site_cap) {
+  const bool pooled = use_pool(c);
+  if (pooled && !c->pool) return fail(ABX_ERR_INVALID, "pooled transport kernel without its slot records");
   if (mixed) {
     TransportArgs<float> A = make_args<float>(c, c->bf[which_bank].b, c->sf.s, site_cap);
-    launch_transport_f(A, kernel_code(c), c->all_iso, c->trace_nhist > 0, c->grid, c->block, c->stream);
+    if (pooled) launch_pool_f(A, kernel_code(c), c->all_iso, c->grid, c->block, c->stream);
+    else launch_transport_f(A, kernel_code(c), c->all_iso, c->trace_nhist > 0, c->grid, c->block, c->stream);
   } else {
     TransportArgs<double> A = make_args<double>(c, c->bd[which_bank].b, c->sd.s, site_cap);
-    launch_transport_d(A, kernel_code(c), c->trace_nhist > 0, c->grid, c->block, c->stream);
+    if (pooled) launch_pool_d(A, kernel_code(c), c->grid, c->block, c->stream);
+    else launch_transport_d(A, kernel_code(c), c->trace_nhist > 0, c->grid, c->block, c->stream);
   }
   CUDA_TRY(cudaGetLastError());
   return ABX_OK;
@@ -911,7 +970,7 @@ static int create_ctx(const abx_problem* problems, int nprob, int device, abx_ct
   int block = problem->settings.block_size > 0 ? problem->settings.block_size : 256;
   block = std::max(32, std::min(256, block / 32 * 32));
   c->block = block;
-  int occ = prec == ABX_PREC_MIXED ? occupancy_f(kernel_code(c), c->all_iso, block) : occupancy_d(kernel_code(c), block);
+  int occ = occupancy_of(c, prec == ABX_PREC_MIXED, block);
   if (occ < 1) occ = 1;
   c->grid = c->nsm * occ;
   if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(ABX_ERR_CUDA, "device sync failed"));
@@ -1091,7 +1150,7 @@ extern "C" int abx_autotune(abx_ctx* c, size_t n_probe, int* block_out, int* gri
   int best_block = block0, best_grid = grid0;
   float best = -1.f;
   for (int block : {128, 256}) {
-    const int occ = mixed ? occupancy_f(kernel_code(c), c->all_iso, block) : occupancy_d(kernel_code(c), block);
+    const int occ = occupancy_of(c, mixed, block);
     for (int per_sm = 1; per_sm <= occ; per_sm++) {
       c->block = block;
       c->grid = c->nsm * per_sm;
@@ -1467,7 +1526,8 @@ static int ensure_gen_graphs(abx_ctx* c, bool mixed, size_t cap, int nignored) {
                                   c->tally_var, c->ent_bins, c->ent_total, c->sec, c->st, c->run, c->gen_rec,
                                   c->D.T.probs, (const void*)(uintptr_t)c->grid, (const void*)(uintptr_t)c->block,
                                   (const void*)(uintptr_t)mixed, (const void*)(uintptr_t)c->hist_cap,
-                                  (const void*)(uintptr_t)c->ent_nbins};
+                                  (const void*)(uintptr_t)c->ent_nbins, c->pool,
+                                  (const void*)(uintptr_t)use_pool(c)};
   if (c->gen_exec[0] && c->gen_cap == cap && c->gen_nignored == nignored && sig == c->gen_sig) return ABX_OK;
   for (auto& e : c->gen_exec)
     if (e) cudaGraphExecDestroy(e);
@@ -1513,6 +1573,28 @@ static int ensure_gen_graphs(abx_ctx* c, bool mixed, size_t cap, int nignored) {
   c->gen_cap = cap;
   c->gen_nignored = nignored;
   c->gen_sig = sig;
+  return ABX_OK;
+}
+
+extern "C" int abx_set_transport_kernel(abx_ctx* c, int kind) {
+  if (!c) return fail(ABX_ERR_INVALID, "null context");
+  if (kind != ABX_TRANSPORT_KERNEL_AUTO && kind != ABX_TRANSPORT_KERNEL_HISTORY && kind != ABX_TRANSPORT_KERNEL_POOL)
+    return fail(ABX_ERR_INVALID, "unknown transport kernel %d", kind);
+  if (kind == ABX_TRANSPORT_KERNEL_POOL && !pool_eligible(c))
+    return fail(ABX_ERR_UNSUPPORTED,
+                "the pooled kernel serves delta and surface tracking without secondary stacks or branchless collisions");
+  cudaSetDevice(c->device);
+  c->kernel_mode = kind;
+  // the launch shape follows the kernel's occupancy
+  int occ = occupancy_of(c, mixed_of(c), c->block);
+  if (occ < 1) occ = 1;
+  c->grid = c->nsm * occ;
+  return ensure_sec(c, mixed_of(c));
+}
+
+extern "C" int abx_get_transport_kernel(abx_ctx* c, int* kind) {
+  if (!c || !kind) return fail(ABX_ERR_INVALID, "bad arguments");
+  *kind = use_pool(c) ? ABX_TRANSPORT_KERNEL_POOL : ABX_TRANSPORT_KERNEL_HISTORY;
   return ABX_OK;
 }
 

@@ -49,6 +49,8 @@ template <class R> struct TransportArgs {
   // counters [prob][ABX_PCOUNTS]; nullptr when one problem runs alone
   double* pscore;
   unsigned long long* pcount;
+  // pooled kernel: 32 * POOL_K slot records per warp of the launch
+  void* pool;
 };
 
 enum : int { ABX_PSCORES = 5, ABX_PCOUNTS = 4 };

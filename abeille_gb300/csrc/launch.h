@@ -56,6 +56,17 @@ int occupancy_f_branchless(int tracking, bool iso, int block);
 int transport_regs_f(int tracking);
 int transport_regs_f_surface();
 
+// transport_pool_mixed.cu / transport_pool_fp64.cu: the pooled kernels
+// (delta tracking, surface tracking); `A.pool` holds pool_slot_bytes_*()
+// bytes for each of the 32 * POOL_K slots of every warp of the launch
+void launch_pool_f(const TransportArgs<float>& A, int tracking, bool iso, int grid, int block, cudaStream_t s);
+int occupancy_pool_f(int tracking, bool iso, int block);
+size_t pool_slot_bytes_f();
+void launch_pool_d(const TransportArgs<double>& A, int tracking, int grid, int block, cudaStream_t s);
+int occupancy_pool_d(int tracking, int block);
+size_t pool_slot_bytes_d();
+constexpr int POOL_SLOTS_PER_WARP = 128;
+
 // occupancy helpers
 int occupancy_d(int tracking, int block);
 int occupancy_f(int tracking, bool iso, int block);

@@ -143,6 +143,18 @@ class Engine:
     def set_graphs(self, enabled):
         self._chk(self.lib.abx_set_graphs(self.ctx, int(bool(enabled))))
 
+    KERNELS = {"auto": 0, "history": 1, "pool": 2}
+
+    def set_transport_kernel(self, kind):
+        """"history": one lane per history; "pool": event-sorted warps over
+        pools of 128 histories; "auto": the engine's choice."""
+        self._chk(self.lib.abx_set_transport_kernel(self.ctx, self.KERNELS[kind]))
+
+    def transport_kernel(self):
+        k = C.c_int()
+        self._chk(self.lib.abx_get_transport_kernel(self.ctx, C.byref(k)))
+        return {1: "history", 2: "pool"}[k.value]
+
     def run_power_iteration(self, ngenerations, nignored):
         st = abi.RunStats()
         k = np.zeros(ngenerations)

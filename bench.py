@@ -231,6 +231,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run of the mixed mode")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "history", "pool"],
+                    help="configs 0-2: transport kernel (history: one lane per history; pool: event-sorted warps)")
     ap.add_argument("--tracking", default=None,
                     choices=["delta-tracking", "surface-tracking", "implicit-leakage-delta-tracking", "carter-tracking"])
     ap.add_argument("--problems", type=int, default=4096, help="config 3: problems in the batch")
@@ -267,9 +269,12 @@ def main():
     builder.seed = builder.seed + 7919 * rank  # independent replica per rank
     eng = Engine(builder.build(precision=args.precision), local)
 
+    if args.kernel != "auto":
+        eng.set_transport_kernel(args.kernel)
     shape = None
     if args.autotune:
         shape = eng.autotune(npart if args.autotune < 0 else args.autotune)
+    kernel_used = eng.transport_kernel()
     # L2 flush between generations, outside each generation's timed events
     from abeille_gb300 import abi as _abi
     _abi.check(eng.lib.abx_set_l2_flush(eng.ctx, L2_FLUSH_BYTES), eng.lib)
@@ -345,7 +350,7 @@ def main():
                    "l2": f"flushed: {L2_FLUSH_BYTES >> 20} MiB written before each generation, outside its "
                    "timed events", "parallelism": f"replicas{world}",
                    "launch": {"autotuned": bool(shape), "block": shape[0] if shape else None,
-                              "grid": shape[1] if shape else None}},
+                              "grid": shape[1] if shape else None, "kernel": kernel_used}},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": KERNELS_PER_GEN * args.steps,
         "clocks": clk.summary(),

@@ -562,6 +562,24 @@ int abx_last_transport_ms(abx_ctx* ctx, double* ms);
  * runs always launch directly. */
 int abx_set_graphs(abx_ctx* ctx, int enabled);
 
+/* Transport kernel (no reference counterpart; results do not depend on it).
+ * HISTORY: one lane per history, the lanes of a warp running their event
+ * machines side by side.  POOL: each warp keeps 128 histories in device
+ * memory and runs one event kind at a time on up to 32 of them (event-sorted
+ * execution inside one persistent launch); delta and surface tracking with
+ * branching collisions only -- Carter tracking, branchless collisions and
+ * problems whose histories carry secondaries (fixed source with fission)
+ * return ABX_ERR_UNSUPPORTED.  AUTO: the engine's choice.  Setting a kernel
+ * resets the launch shape to that kernel's full occupancy. */
+enum {
+  ABX_TRANSPORT_KERNEL_AUTO = 0,
+  ABX_TRANSPORT_KERNEL_HISTORY = 1,
+  ABX_TRANSPORT_KERNEL_POOL = 2
+};
+int abx_set_transport_kernel(abx_ctx* ctx, int kind);
+/* The kernel the next transport launch uses (HISTORY or POOL). */
+int abx_get_transport_kernel(abx_ctx* ctx, int* kind);
+
 /* Launch-shape autotuner (no reference counterpart): transports the same
  * `n_probe` first-generation source histories three times per candidate
  * shape (128 or 256 threads per block, 1 .. the occupancy limit of blocks per
