@@ -276,6 +276,18 @@ int append_problem(Pools& P, const abx_problem* pr) {
     const double* sct = chi + (size_t)G * G;
     const double* legm = sct + (size_t)G * G;
     const double* dgp = legm + (size_t)mt.n_legendre * G * G;
+    // the input checks of make_mg_nuclide (src/mg_nuclide.cpp:604-636, 720-738, 826-834)
+    for (int g = 0; g < G; g++) {
+      if (fis[g] < 0.) return fail(ABX_ERR_INVALID, "Negative fission xs in material %u.", mt.id);
+      for (int o = 0; o < G; o++) {
+        if (sct[(size_t)g * G + o] < 0.)
+          return fail(ABX_ERR_INVALID,
+                      "Negative scattering component at row %d, column %d of the scattering matrix for material %u.",
+                      g, o, mt.id);
+        if (chi[(size_t)g * G + o] < 0.)
+          return fail(ABX_ERR_INVALID, "chi[%d][%d] is negative in material %u.", g, o, mt.id);
+      }
+    }
     MatT M{};
     M.G = G;
     M.xs_off = (int)P.xs_d.size();
@@ -338,6 +350,11 @@ int append_problem(Pools& P, const abx_problem* pr) {
         const std::vector<double> a(ac, ac + mt.n_legendre + 1);
         std::vector<double> mu, pp, cc;
         if (!linearize(a, mu, pp, cc)) return fail(ABX_ERR_INVALID, "material %u: angle table did not converge", mt.id);
+        // MGAngleDistribution's check (src/mg_angle_distribution.cpp:53-58)
+        for (double p : pp)
+          if (p < 0.)
+            return fail(ABX_ERR_INVALID, "material %u: the angle distribution from group %d to group %d has a "
+                        "negative pdf (PDF is less than 0)", mt.id, gi, go);
         bool iso = mu.size() == 2 && pp[0] == 0.5 && pp[1] == 0.5 && cc[0] == 0. && cc[1] == 1.;
         if (!iso) M.iso = 0;
         h.n = (int)mu.size();

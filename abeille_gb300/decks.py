@@ -48,6 +48,10 @@ def _downscatter_matrix(rng, sig_s, frac_down, G, upscatter_from=None, up_frac=0
         fu = 0.0
         if upscatter_from is not None and g > upscatter_from:
             fu = up_frac
+            # keep the in-group element non-negative (the reference refuses
+            # negative scattering components, src/mg_nuclide.cpp:628-634)
+            if fd + fu > 0.99:
+                fd = 0.99 - fu
             above = np.arange(upscatter_from, g)
             wu = 0.5 ** (g - above - 1) * (0.8 + 0.4 * rng.random(above.size))
             wu /= wu.sum()
@@ -199,13 +203,14 @@ def quadrics(nparticles=4096, precision="fp64", tracking="delta-tracking", legen
     """Spheres, general planes (normals off the axes, one of them a reflective
     boundary) and x/y-cylinders, the surface kinds the lattice configurations
     do not use (src/sphere.cpp, src/plane.cpp, src/xcylinder.cpp,
-    src/ycylinder.cpp).  With `legendre`, the moderator scatters with a P1
-    moment (mean cosine 0.2), so angle tables are sampled as well."""
+    src/ycylinder.cpp).  With `legendre`, the moderator scatters with mean
+    cosine 0.2 (a P1 entry), so angle tables are sampled as well."""
     fuel, mod, water = seven_group_xs()
     b = ProblemBuilder(7, np.arange(8.0), nparticles=nparticles, precision=precision, tracking=tracking)
     b.material(1, **fuel)
     if legendre:
-        mod = dict(mod, legendre={1: 0.2 * np.asarray(mod["scatter"])})
+        # P1 entries are mean scattering cosines (pdf 1/2 + 3/2 mu_bar mu)
+        mod = dict(mod, legendre={1: 0.2 * (np.asarray(mod["scatter"]) > 0)})
     b.material(2, **mod)
     b.material(3, **water)
     b.surface("sphere", 1, x0=0.0, y0=0.0, z0=0.0, r=3.0)
@@ -356,7 +361,10 @@ def from_reference_deck(deck, nparticles=None, precision="fp64", tracking=None):
         b.source(kind, position=sp.get("position"), low=sp.get("low"), hi=sp.get("hi"),
                  direction="isotropic" if dr["type"] == "isotropic" else "mono-directional",
                  direction_vector=dr.get("direction"), energy=float(en["energy"]), weight=float(s["weight"]),
-                 fissile_only=bool(sp.get("fissile-only", False)))
+                 # read at the source entry, as src/source.cpp:104-110 does (a
+                 # `fissile-only` inside `spatial`, as input_files/c5g7.yaml:321
+                 # has it, is not read by the reference)
+                 fissile_only=bool(s.get("fissile-only", False)))
     for t in deck.get("tallies", []):
         b.mesh_tally(t["shape"], t["low"], t["hi"], t.get("estimator", "collision"), t.get("quantity", "flux"),
                      t.get("energy-bounds"))

@@ -288,20 +288,25 @@ class ProblemBuilder:
         for so in self.sources:
             sp = ({"type": "point", "position": [so.low[a] for a in range(3)]} if so.spatial == abi.SPATIAL["point"]
                   else {"type": "box", "low": [so.low[a] for a in range(3)], "hi": [so.hi[a] for a in range(3)]})
-            if so.fissile_only:
-                sp["fissile-only"] = True
             dr = ({"type": "isotropic"} if so.direction == abi.DIRECTION["isotropic"]
                   else {"type": "mono-directional", "direction": [so.dir[a] for a in range(3)]})
-            srcs.append({"spatial": sp, "direction": dr, "energy": {"type": "mono-energetic",
-                                                                    "energy": so.energy_value},
-                         "weight": so.weight})
+            src = {"spatial": sp, "direction": dr, "energy": {"type": "mono-energetic", "energy": so.energy_value},
+                   "weight": so.weight}
+            if so.fissile_only:  # a key of the source entry (src/source.cpp:104-110)
+                src["fissile-only"] = True
+            srcs.append(src)
         est = {v: k for k, v in abi.EST.items()}
         qty = {v: k for k, v in abi.QUANTITY.items()}
-        tallies = [{"shape": t["shape"], "low": t["low"], "hi": t["hi"], "estimator": est[t["est"]],
-                    "quantity": qty[t["q"]], "energy-bounds": np.asarray(t["eb"]).tolist()} for t in self.tallies]
+        # every mesh tally needs a unique name (src/collision_mesh_tally.cpp:210-230)
+        tallies = [{"name": f"tally{i}", "shape": t["shape"], "low": t["low"], "hi": t["hi"],
+                    "estimator": est[t["est"]], "quantity": qty[t["q"]],
+                    "energy-bounds": np.asarray(t["eb"]).tolist()} for i, t in enumerate(self.tallies)]
         settings = {"nparticles": int(self.nparticles), "ngroups": G, "transport": self.tracking,
                     "simulation": self.mode, "energy-mode": "multi-group",
                     "energy-bounds": self.energy_bounds.tolist(), "seed": int(self.seed), "stride": int(self.stride)}
+        settings["wgt-cutoff"] = float(self.wgt_cutoff)
+        settings["wgt-survival"] = float(self.wgt_survival)
+        settings["wgt-split"] = float(self.wgt_split)
         if self.mode == "branchless-k-eigenvalue":
             settings["branchless-material"] = self.branchless_material
             settings["branchless-splitting"] = self.branchless_splitting
@@ -316,6 +321,8 @@ class ProblemBuilder:
             deck["tallies"] = tallies
         if self.entropy:
             deck["entropy"] = dict(self.entropy)
+        if self.sampling_xs_ratio is not None:
+            deck["sampling-xs-ratio"] = list(self.sampling_xs_ratio)  # a top-level key (src/parser.cpp:425-434)
         deck["settings"] = settings
         return deck
 

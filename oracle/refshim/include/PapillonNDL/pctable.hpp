@@ -1,0 +1,2 @@
+#pragma once
+#include <PapillonNDL/stub_common.hpp>

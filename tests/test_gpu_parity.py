@@ -328,24 +328,54 @@ def test_errors_leave_the_context_usable():
         eng.transport(bank, 1.0, True, site_capacity=1)
 
 
+def _t_frac(dof):
+    """P(|t| < 2) for Student's t with `dof` degrees of freedom: the expected
+    fraction of bins with |z| < 2 when both sides sample one distribution."""
+    from scipy import stats
+    return float(stats.t.cdf(2, dof) - stats.t.cdf(-2, dof))
+
+
 def test_mixed_precision_statistics_config1():
-    """Config 1 (51x51 pins, 10 axial zones, 51x51x20 flux tally) at 2e5
-    histories per generation, 10 inactive + 40 active generations: the mixed
-    mode against FP64 over independent replicas, with an FP64/FP64 control
-    (same criteria as config 0)."""
-    R = 12
-    mk = lambda: decks.config1(nparticles=200000)  # noqa: E731
-    fp64_a = _replicas(mk, "fp64", 5000, R, 50, 10)
-    fp64_b = _replicas(mk, "fp64", 7000, R // 2, 50, 10)
-    mixed = _replicas(mk, "mixed", 9000, R, 50, 10)
-    keep = (fp64_a[1].mean(0) > 0) & (mixed[1].mean(0) > 0)
-    dk, frac, mz = _agreement(mixed, fp64_a, keep)
-    dk_c, frac_c, mz_c = _agreement(fp64_b, fp64_a, keep)
-    print(f"config 1 mixed vs fp64: dk = {dk:.2f} sigma, {frac:.3f} of {keep.sum()} bins |z| < 2, mean z {mz:+.3f}; "
-          f"fp64 vs fp64 control: dk = {dk_c:.2f}, {frac_c:.3f}, mean z {mz_c:+.3f}")
+    """The acceptance check of the FP32-tracking / FP64-tally mode on config 1
+    (51x51 pins, 10 axial zones, 51x51x20 flux tally): k within 2 sigma and
+    flux bins with |z| < 2, mixed against FP64, over independent replicas.
+
+    Two sets of 32 replicas per precision (5e4 histories, 10 inactive + 40
+    active generations each) give four mixed/FP64 pairs of sets (62 degrees
+    of freedom per pair) and one pooled comparison (64 against 64 replicas,
+    126 degrees of freedom).  For two samples of one distribution the
+    fraction of bins with |z| < 2 is the t-distribution's P(|t| < 2): 0.950
+    per pair, 0.952 pooled -- the spec bar of 95 % sits at that
+    expectation.  All bins share one fission source, so the fraction of one
+    comparison moves by about a percent around it (FP64 against FP64 as
+    well: a 4x40-replica study gave mixed/FP64 pairs 0.941-0.965, mean
+    0.954, FP64/FP64 pairs 0.947-0.968).  The test therefore asserts the
+    pooled fraction and the mean over pairs against the expectation less one
+    percent, and the same FP64/FP64 control; the 95 % bar itself is read from
+    `bench.py --zscore`, which compares many more replicas."""
+    R, n = 32, 50000
+    mk = lambda: decks.config1(nparticles=n)  # noqa: E731
+    sets = {}
+    for si in range(2):
+        sets[f"fp64{si}"] = _replicas(mk, "fp64", 30000 + 1000 * si, R, 50, 10)
+        sets[f"mixed{si}"] = _replicas(mk, "mixed", 40000 + 1000 * si, R, 50, 10)
+    keep = np.all([v[1].mean(0) > 0 for v in sets.values()], axis=0)
+    pairs = [_agreement(sets[f"mixed{a}"], sets[f"fp64{b}"], keep) for a in range(2) for b in range(2)]
+    pool = lambda p: (np.concatenate([sets[f"{p}{i}"][0] for i in range(2)]),  # noqa: E731
+                      np.concatenate([sets[f"{p}{i}"][1] for i in range(2)]))
+    dk, frac, mz = _agreement(pool("mixed"), pool("fp64"), keep)
+    _, frac_c, _ = _agreement(sets["fp641"], sets["fp640"], keep)
+    mean_pairs = float(np.mean([p[1] for p in pairs]))
+    print(f"config 1 mixed vs fp64 pooled: dk = {dk:.2f} sigma, {frac:.4f} of {keep.sum()} bins |z| < 2 "
+          f"(expected {_t_frac(4 * R - 2):.4f}), mean z {mz:+.3f}; pairs: "
+          f"{[round(p[1], 4) for p in pairs]} mean {mean_pairs:.4f} (expected {_t_frac(2 * R - 2):.4f}); "
+          f"fp64/fp64 control {frac_c:.4f}")
     assert abs(dk) < 2, dk
-    assert frac >= 0.85 and frac >= frac_c - 0.08, (frac, frac_c)
-    assert abs(mz) < 0.3, mz
+    assert all(abs(p[0]) < 2 for p in pairs), pairs
+    assert frac >= _t_frac(4 * R - 2) - 0.01, frac
+    assert mean_pairs >= _t_frac(2 * R - 2) - 0.01, mean_pairs
+    assert mean_pairs >= frac_c - 0.02, (mean_pairs, frac_c)
+    assert abs(mz) < 0.1, mz
 
 
 @pytest.mark.parametrize("tracking", ["surface-tracking", "delta-tracking"])
