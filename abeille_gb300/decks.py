@@ -199,12 +199,20 @@ def seventy_group_xs(seed=1, nfuel=8):
     return mats
 
 
-def quadrics(nparticles=4096, precision="fp64", tracking="delta-tracking", legendre=False):
-    """Spheres, general planes (normals off the axes, one of them a reflective
-    boundary) and x/y-cylinders, the surface kinds the lattice configurations
-    do not use (src/sphere.cpp, src/plane.cpp, src/xcylinder.cpp,
-    src/ycylinder.cpp).  With `legendre`, the moderator scatters with mean
-    cosine 0.2 (a P1 entry), so angle tables are sampled as well."""
+def quadrics(nparticles=4096, precision="fp64", tracking="delta-tracking", legendre=False, cap="reflective"):
+    """Spheres, general planes (normals off the axes, one of them a boundary
+    condition, reflective by default) and x/y-cylinders, the surface kinds the
+    lattice configurations do not use (src/sphere.cpp, src/plane.cpp,
+    src/xcylinder.cpp, src/ycylinder.cpp).  With `legendre`, the moderator
+    scatters with mean cosine 0.2 (a P1 entry), so angle tables are sampled as
+    well.
+
+    A reflective general plane is where the reference's own arithmetic is
+    most fragile: Plane::distance (src/plane.cpp:47-59) compares the distance,
+    not the position, with SURFACE_COINCIDENT, so a particle reflected at
+    grazing incidence and left a rounding error on the far side of the plane
+    can find it again a few 1e-12 cm away and be lost.  Runs of very many
+    FP64 histories use `cap="vacuum"`."""
     fuel, mod, water = seven_group_xs()
     b = ProblemBuilder(7, np.arange(8.0), nparticles=nparticles, precision=precision, tracking=tracking)
     b.material(1, **fuel)
@@ -218,7 +226,7 @@ def quadrics(nparticles=4096, precision="fp64", tracking="delta-tracking", legen
     b.surface("ycylinder", 3, x0=-6.0, z0=-3.0, r=1.5)
     b.surface("plane", 4, A=0.6, B=0.48, C=0.64, D=1.5)
     b.surface("sphere", 5, x0=0.0, y0=0.0, z0=0.0, r=11.0, boundary="vacuum")
-    b.surface("plane", 6, A=0.3, B=-0.4, C=0.8660254037844386, D=5.0, boundary="reflective")
+    b.surface("plane", 6, A=0.3, B=-0.4, C=0.8660254037844386, D=5.0, boundary=cap)
     b.cell(1, "-1", material=1)
     b.cell(2, "-2 & -5 & -6", material=1)
     b.cell(3, "-3 & -5 & -6", material=3)
