@@ -151,7 +151,8 @@ class ProblemResult(C.Structure):
 
 class ServerOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("tracking", C.c_int32), ("nbatches", C.c_int32),
-                ("hbm_budget_bytes", C.c_uint64), ("max_round_problems", C.c_int32), ("keep_tallies", C.c_int32)]
+                ("hbm_budget_bytes", C.c_uint64), ("max_round_problems", C.c_int32), ("keep_tallies", C.c_int32),
+                ("lanes", C.c_int32), ("history_quantum", C.c_uint32)]
 
 
 class RequestResult(C.Structure):
@@ -197,6 +198,10 @@ PROTOTYPES = {
     "abx_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "abx_set_transport_kernel": (C.c_int, [C.c_void_p, C.c_int]),
     "abx_get_transport_kernel": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "abx_set_history_quantum": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "abx_deck_read": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.POINTER(Problem))]),
+    "abx_deck_free": (C.c_int, [C.c_void_p]),
+    "abx_create_from_deck": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "abx_autotune": (C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                C.POINTER(C.c_double)]),
     "abx_create_batch": (C.c_int, [C.POINTER(Problem), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),

@@ -57,6 +57,11 @@ extern "C" int abx_version(int* a, int* b, int* c) {
 }
 
 // ------------------------------------------------------------ device pools
+// Buffers that follow the size of the work grow by half again when they must
+// grow: every reallocation frees device memory, and cudaFree waits for the
+// whole device -- in the request loop, for the launches of the other lanes.
+static size_t headroom(size_t n) { return n + n / 2; }
+
 // Device copies of the pools.  upload() fills the slots in a fixed order, so
 // a context whose problems are replaced reuses each slot's allocation when it
 // is large enough.
@@ -75,8 +80,8 @@ struct DevPools {
       if (allocs[slot]) cudaFree(allocs[slot]);
       allocs[slot] = nullptr;
       caps[slot] = 0;
-      CUDA_TRY(cudaMalloc(&allocs[slot], bytes));
-      caps[slot] = bytes;
+      CUDA_TRY(cudaMalloc(&allocs[slot], headroom(bytes)));
+      caps[slot] = headroom(bytes);
     }
     void* p = allocs[slot++];
     if (!v.empty()) CUDA_TRY(cudaMemcpy(p, v.data(), v.size() * sizeof(X), cudaMemcpyHostToDevice));
@@ -96,6 +101,19 @@ template <class X> static std::vector<float> to_f(const std::vector<X>& v) {
   std::vector<float> o(v.size());
   for (size_t i = 0; i < v.size(); i++) o[i] = (float)v[i];
   return o;
+}
+
+// Table uploads are synchronous copies on the legacy stream, which is not
+// ordered with the context's (non-blocking) stream: make the stream wait for
+// them before it runs kernels that read the tables (other contexts' streams
+// keep running meanwhile).
+static int after_host_copies(cudaStream_t s) {
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return ABX_ERR_CUDA;
+  cudaError_t r = cudaEventRecord(e, 0);
+  if (r == cudaSuccess) r = cudaStreamWaitEvent(s, e, 0);
+  cudaEventDestroy(e);
+  return r == cudaSuccess ? ABX_OK : ABX_ERR_CUDA;
 }
 
 static int upload(const Pools& P, DevPools& D) {
@@ -322,6 +340,10 @@ struct abx_context {
   int kernel_mode = ABX_TRANSPORT_KERNEL_AUTO;
   void* pool = nullptr;
   size_t pool_bytes = 0;
+  // batch runs: histories per warp before it retires (0: persistent warps),
+  // and the quota of the launch being made
+  uint32_t warp_quota = 0;
+  uint32_t launch_quota = 0;
 };
 
 static void ctx_free(abx_ctx* c) {
@@ -714,7 +736,7 @@ __global__ void k_sites_to_aos(SiteT<R> S, const DevState* st, const uint32_t* o
 
 static int ensure_counts(abx_ctx* c, size_t n) {
   if (n <= c->count_cap) return ABX_OK;
-  size_t cap = std::max<size_t>(n, 1024);
+  size_t cap = std::max<size_t>(headroom(n), 1024);
   if (c->hist_count) cudaFree(c->hist_count);
   if (c->offsets) cudaFree(c->offsets);
   if (c->block_sums) cudaFree(c->block_sums);
@@ -732,9 +754,9 @@ static int ensure_banks(abx_ctx* c, size_t n, bool mixed, bool with_prob) {
   // banks of the transport precision only (mixed runs sample in FP32)
   for (int i = 0; i < 2; i++) {
     if (!mixed && (c->bd[i].cap < n || (with_prob && !c->bd[i].b.prob)))
-      if ((rc = c->bd[i].alloc(n, with_prob)) != ABX_OK) return rc;
+      if ((rc = c->bd[i].alloc(headroom(n), with_prob)) != ABX_OK) return rc;
     if (mixed && (c->bf[i].cap < n || (with_prob && !c->bf[i].b.prob)))
-      if ((rc = c->bf[i].alloc(n, with_prob)) != ABX_OK) return rc;
+      if ((rc = c->bf[i].alloc(headroom(n), with_prob)) != ABX_OK) return rc;
   }
   return ensure_counts(c, n);
 }
@@ -742,9 +764,9 @@ static int ensure_banks(abx_ctx* c, size_t n, bool mixed, bool with_prob) {
 static int ensure_sites(abx_ctx* c, size_t n, bool mixed) {
   int rc;
   if (mixed) {
-    if (c->sf.cap < n && (rc = c->sf.alloc(n)) != ABX_OK) return rc;
+    if (c->sf.cap < n && (rc = c->sf.alloc(headroom(n))) != ABX_OK) return rc;
   } else {
-    if (c->sd.cap < n && (rc = c->sd.alloc(n)) != ABX_OK) return rc;
+    if (c->sd.cap < n && (rc = c->sd.alloc(headroom(n))) != ABX_OK) return rc;
   }
   return ABX_OK;
 }
@@ -864,6 +886,7 @@ template <class R> static TransportArgs<R> make_args(abx_ctx* c, const BankT<R>&
   A.pscore = c->batch_scores ? c->pscore : nullptr;
   A.pcount = c->batch_scores ? c->pcount : nullptr;
   A.pool = use_pool(c) ? c->pool : nullptr;
+  A.warp_quota = c->launch_quota;
   return A;
 }
 
@@ -1592,6 +1615,12 @@ extern "C" int abx_set_transport_kernel(abx_ctx* c, int kind) {
   return ensure_sec(c, mixed_of(c));
 }
 
+extern "C" int abx_set_history_quantum(abx_ctx* c, uint32_t histories_per_warp) {
+  if (!c) return fail(ABX_ERR_INVALID, "null context");
+  c->warp_quota = histories_per_warp;
+  return ABX_OK;
+}
+
 extern "C" int abx_get_transport_kernel(abx_ctx* c, int* kind) {
   if (!c || !kind) return fail(ABX_ERR_INVALID, "bad arguments");
   *kind = use_pool(c) ? ABX_TRANSPORT_KERNEL_POOL : ABX_TRANSPORT_KERNEL_HISTORY;
@@ -2127,22 +2156,23 @@ static int abx::install_prepared(abx_ctx* c, PreparedBatch* b) {
   for (const MatT& m : c->P.mats) c->all_iso = c->all_iso && m.iso != 0;
   int rc = upload(c->P, c->D);
   if (rc) return rc;
+  if (after_host_copies(c->stream) != ABX_OK) return fail(ABX_ERR_CUDA, "stream ordering of the table upload failed");
   const size_t R = (size_t)std::max<int64_t>(c->P.tally_bins, 1);
   if (c->tally_rv_cap < R) {
     cudaFree(c->tally_avg);
     cudaFree(c->tally_var);
     c->tally_avg = c->tally_var = nullptr;
     c->tally_rv_cap = 0;
-    CUDA_TRY(cudaMalloc(&c->tally_avg, R * 8));
-    CUDA_TRY(cudaMalloc(&c->tally_var, R * 8));
-    c->tally_rv_cap = R;
+    CUDA_TRY(cudaMalloc(&c->tally_avg, headroom(R) * 8));
+    CUDA_TRY(cudaMalloc(&c->tally_var, headroom(R) * 8));
+    c->tally_rv_cap = headroom(R);
   }
   if (c->tally_gen_cap < R) {
     cudaFree(c->tally_gen);
     c->tally_gen = nullptr;
     c->tally_gen_cap = 0;
-    CUDA_TRY(cudaMalloc(&c->tally_gen, R * 8));
-    c->tally_gen_cap = R;
+    CUDA_TRY(cudaMalloc(&c->tally_gen, headroom(R) * 8));
+    c->tally_gen_cap = headroom(R);
   }
   zero_d(c->tally_gen, R, c->stream);
   zero_d(c->tally_avg, R, c->stream);
@@ -2184,8 +2214,8 @@ static int ensure_virtual(abx_ctx* c, int nb) {
     if (*ptr) cudaFree(*ptr);
     *ptr = nullptr;
     *cap = 0;
-    CUDA_TRY(cudaMalloc(ptr, bytes));
-    *cap = bytes;
+    CUDA_TRY(cudaMalloc(ptr, headroom(bytes)));
+    *cap = headroom(bytes);
     return ABX_OK;
   };
   const size_t nv = (size_t)np * nb;
@@ -2206,8 +2236,8 @@ static int ensure_virtual(abx_ctx* c, int nb) {
     if (c->tally_gen) cudaFree(c->tally_gen);
     c->tally_gen = nullptr;
     c->tally_gen_cap = 0;
-    CUDA_TRY(cudaMalloc(&c->tally_gen, need * 8));
-    c->tally_gen_cap = need;
+    CUDA_TRY(cudaMalloc(&c->tally_gen, headroom(need) * 8));
+    c->tally_gen_cap = headroom(need);
   }
   // segments: virtual problem v = p*nb + b holds histories b*n_p .. (b+1)*n_p-1
   std::vector<uint64_t> off(nv + 1), hid0(nv);
@@ -2248,6 +2278,7 @@ extern "C" int abx_run_fixed_source_batch(abx_ctx* c, int nbatches, abx_problem_
     return fail(ABX_ERR_CAPACITY, "%llu histories in one launch", (unsigned long long)total);
   int rc;
   if ((rc = ensure_virtual(c, nbatches)) != ABX_OK) return rc;
+  if (after_host_copies(c->stream) != ABX_OK) return fail(ABX_ERR_CUDA, "stream ordering of the batch layout failed");
   if ((rc = ensure_banks(c, total, mixed, true)) != ABX_OK) return rc;
   if ((rc = ensure_sites(c, 1, mixed)) != ABX_OK) return rc;
   if ((rc = ensure_sec(c, mixed)) != ABX_OK) return rc;
@@ -2279,7 +2310,19 @@ extern "C" int abx_run_fixed_source_batch(abx_ctx* c, int nbatches, abx_problem_
   cudaEventRecord(ev[1], c->stream);
   c->batch_tables = TV;
   c->batch_scores = true;
+  // with a history quota, warps retire after `warp_quota` histories and the
+  // grid grows to cover the launch: blocks finish and hand their SM slots
+  // to the launches of other contexts' streams while this one runs
+  const int grid0 = c->grid;
+  if (c->warp_quota && !needs_stacks(c) && !use_pool(c)) {
+    const uint64_t per_block = (uint64_t)c->warp_quota * (uint64_t)(c->block / 32);
+    const uint64_t need_blocks = (total + per_block - 1) / per_block;
+    if (need_blocks > (uint64_t)c->grid) c->grid = (int)std::min<uint64_t>(need_blocks, 0x7fffffffull);
+    c->launch_quota = c->warp_quota;
+  }
   rc = launch_transport(c, mixed, 0, 0);
+  c->launch_quota = 0;
+  c->grid = grid0;
   c->batch_scores = false;
   cudaEventRecord(ev[2], c->stream);
   if (rc == ABX_OK) {

@@ -51,6 +51,12 @@ template <class R> struct TransportArgs {
   unsigned long long* pcount;
   // pooled kernel: 32 * POOL_K slot records per warp of the launch
   void* pool;
+  // history kernel: histories a warp takes before it retires (0: no limit).
+  // With a grid larger than the GPU holds at once, blocks then finish and
+  // leave their SM slots to later blocks -- and to launches of other
+  // streams -- while the launch runs; the grid must cover the histories
+  // (grid * warps per block * quota >= histories).
+  uint32_t warp_quota;
 };
 
 enum : int { ABX_PSCORES = 5, ABX_PCOUNTS = 4 };

@@ -1,19 +1,26 @@
 // Request loop for fixed-source problems: a host scheduler over the C-ABI.
 //
 // Submission copies the problem (the caller's buffers are not retained) and
-// queues it with an estimate of its device footprint.  Rounds go through two
-// threads.  The preparation thread admits queued requests in arrival order
-// while the sum of their footprints fits the HBM budget and derives the
-// round's tables on the host; the GPU thread installs a prepared round into
-// its batch context (created on the first round, its device buffers reused
-// afterwards), runs every batch of every admitted request in one transport
-// launch, and copies results and tally bins back.  The next round is prepared
-// while the current one runs on the GPU.  Requests that arrive meanwhile wait
-// for a later round, so the rounds size themselves to the arrival rate.
+// queues it with an estimate of its device footprint.  A preparation thread
+// admits queued requests in arrival order into a round while the footprints
+// of everything admitted and not yet finished fit the HBM budget, and
+// derives the round's tables on the host.  Several GPU lanes -- threads
+// that each own a batch context, hence its own CUDA stream and device
+// buffers -- take prepared rounds as they come free: a lane installs the
+// round's tables, runs every batch of every request of the round in one
+// transport launch, and copies results and tally bins back.  Rounds of
+// different lanes run on the device at the same time.  Their launches use a
+// history quantum: each warp retires after a bounded number of histories
+// and the grid covers the rest with later blocks, so blocks finish all
+// through a launch and the SM slots they free go to whichever launch is
+// waiting -- a round admitted while others run starts on the device as
+// slots free up, instead of after them.  A request's HBM share returns to
+// the budget when its round completes.
 //
-// A request's results do not depend on its round: batch b of a problem
-// always transports its histories b*n .. (b+1)*n-1, each seeded by skip-ahead
-// on the problem's own stream, and its tallies and scores are its own.
+// A request's results do not depend on its round or lane: batch b of a
+// problem always transports its histories b*n .. (b+1)*n-1, each seeded by
+// skip-ahead on the problem's own stream, and its tallies and scores are its
+// own.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -135,6 +142,7 @@ struct Round {
   std::vector<Request> reqs;
   void* prepared = nullptr;  // host tables of the batch
   int number = 0;
+  uint64_t bytes = 0;        // admitted footprint, returned when the round ends
   Clock::time_point t_admit;
   double prep_ms = 0.;
 };
@@ -151,18 +159,20 @@ struct abx_server {
   uint64_t next_id = 1;
   bool stop = false;
   abx_server_stats stats{};
-  std::thread worker, preparer;
+  std::vector<std::thread> lanes;
+  std::thread preparer;
   int round = 0;
-  abx_ctx* ctx = nullptr;  // owned by the GPU thread
-  std::unique_ptr<Round> staged;  // prepared, waiting for the GPU thread
+  uint64_t inflight_bytes = 0;    // footprint of admitted, unfinished requests
+  int idle_lanes = 0;
+  std::unique_ptr<Round> staged;  // prepared, waiting for a lane
   bool prep_done = false;         // the preparation thread has exited
   std::condition_variable cv_staged;
 
-  void run_round(Round& rd);
+  void run_round(Round& rd, abx_ctx*& ctx);
   void finish(Request& q, Done&& d, double queue_ms);
   void fail_request(Request& q, int status, double queue_ms);
   void prep_loop();
-  void loop();
+  void lane_loop();
 };
 
 void abx_server::fail_request(Request& q, int status, double queue_ms) {
@@ -185,7 +195,7 @@ void abx_server::finish(Request& q, Done&& d, double queue_ms) {
   cv_done.notify_all();
 }
 
-void abx_server::run_round(Round& rd) {
+void abx_server::run_round(Round& rd, abx_ctx*& ctx) {
   std::vector<Request>& reqs = rd.reqs;
   const int n = (int)reqs.size();
   const Clock::time_point t_start = rd.t_admit;
@@ -199,6 +209,7 @@ void abx_server::run_round(Round& rd) {
     std::vector<abx_problem> arr((size_t)n);
     for (int i = 0; i < n; i++) arr[(size_t)i] = reqs[(size_t)i].prob->p;
     rc = abx_create_batch(arr.data(), n, opt.device, &ctx);
+    if (rc == ABX_OK) rc = abx_set_history_quantum(ctx, opt.history_quantum);
   }
   rd.prepared = nullptr;
   const Clock::time_point c1 = Clock::now();
@@ -271,18 +282,25 @@ void abx_server::prep_loop() {
     std::unique_ptr<Round> rd(new Round());
     {
       std::unique_lock<std::mutex> lk(mu);
-      cv_work.wait(lk, [&] { return stop || (!queue.empty() && !staged); });
+      // a round is formed when a lane can take it and the first queued
+      // request fits next to what is already on the device
+      auto can_admit = [&] {
+        return !queue.empty() && !staged && idle_lanes > 0 &&
+               (inflight_bytes == 0 || inflight_bytes + queue.front().footprint <= opt.hbm_budget_bytes);
+      };
+      cv_work.wait(lk, [&] { return stop || can_admit(); });
       if (stop) break;
-      uint64_t used = 0;
       while (!queue.empty()) {
         const Request& h = queue.front();
-        if (!rd->reqs.empty() && used + h.footprint > opt.hbm_budget_bytes) break;
+        if (!rd->reqs.empty() && inflight_bytes + h.footprint > opt.hbm_budget_bytes) break;
         if (opt.max_round_problems > 0 && (int)rd->reqs.size() >= opt.max_round_problems) break;
-        used += h.footprint;
+        inflight_bytes += h.footprint;
+        rd->bytes += h.footprint;
         rd->reqs.push_back(std::move(queue.front()));
         queue.pop_front();
       }
       rd->number = ++round;
+      idle_lanes--;  // reserved for this round
     }
     rd->t_admit = Clock::now();
     int rc = ABX_OK;
@@ -301,9 +319,21 @@ void abx_server::prep_loop() {
       rd->reqs = std::move(good);
       rc = ABX_OK;
       rd->prepared = rd->reqs.empty() ? nullptr : prepare(rd->reqs, &rc);
-      if (rd->reqs.empty()) continue;
-      if (rc != ABX_OK) {
+      if (!rd->reqs.empty() && rc != ABX_OK) {
         for (Request& q : rd->reqs) fail_request(q, rc, ms_between(q.t_submit, rd->t_admit));
+        rd->reqs.clear();
+      }
+      // the failed requests' footprints go back to the budget
+      uint64_t kept = 0;
+      for (const Request& q : rd->reqs) kept += q.footprint;
+      {
+        std::lock_guard<std::mutex> g(mu);
+        inflight_bytes -= rd->bytes - kept;
+        rd->bytes = kept;
+        if (rd->reqs.empty()) idle_lanes++;
+      }
+      if (rd->reqs.empty()) {
+        cv_work.notify_all();
         continue;
       }
     }
@@ -317,8 +347,11 @@ void abx_server::prep_loop() {
   cv_staged.notify_all();
 }
 
-// GPU thread: runs the prepared rounds one after the other.
-void abx_server::loop() {
+// GPU lane: takes prepared rounds as they come and runs them in its own
+// batch context (own stream, own device buffers), concurrently with the
+// other lanes.
+void abx_server::lane_loop() {
+  abx_ctx* ctx = nullptr;
   for (;;) {
     std::unique_ptr<Round> rd;
     {
@@ -329,28 +362,42 @@ void abx_server::loop() {
       cv_work.notify_all();  // the preparation thread may stage the next round
     }
     const Clock::time_point t0 = Clock::now();
-    run_round(*rd);
-    std::lock_guard<std::mutex> g(mu);
-    stats.busy_ms += ms_between(t0, Clock::now());
+    run_round(*rd, ctx);
+    {
+      std::lock_guard<std::mutex> g(mu);
+      stats.busy_ms += ms_between(t0, Clock::now());
+      inflight_bytes -= rd->bytes;  // the round's HBM share is free again
+      idle_lanes++;
+    }
+    cv_work.notify_all();
   }
   if (ctx) abx_destroy(ctx);
-  ctx = nullptr;
-  // cancel what is still queued
-  std::lock_guard<std::mutex> g(mu);
-  while (!queue.empty()) {
-    Request q = std::move(queue.front());
-    queue.pop_front();
+}
+
+// After the lanes stop: cancel what is still queued or staged.
+static void cancel_queued(abx_server* s) {
+  std::lock_guard<std::mutex> g(s->mu);
+  std::vector<Request> left;
+  while (!s->queue.empty()) {
+    left.push_back(std::move(s->queue.front()));
+    s->queue.pop_front();
+  }
+  if (s->staged) {
+    for (Request& q : s->staged->reqs) left.push_back(std::move(q));
+    s->staged->reqs.clear();
+  }
+  for (Request& q : left) {
     Done d;
     d.r.request_id = q.id;
     d.r.tag = q.tag;
     d.r.status = ABX_ERR_CANCELLED;
     d.r.latency_ms = ms_between(q.t_submit, Clock::now());
-    stats.completed++;
-    stats.failed++;
-    ready.push_back(q.id);
-    results.emplace(q.id, std::move(d));
+    s->stats.completed++;
+    s->stats.failed++;
+    s->ready.push_back(q.id);
+    s->results.emplace(q.id, std::move(d));
   }
-  cv_done.notify_all();
+  s->cv_done.notify_all();
 }
 
 extern "C" int abx_server_create(const abx_server_options* options, abx_server** out) {
@@ -361,10 +408,14 @@ extern "C" int abx_server_create(const abx_server_options* options, abx_server**
     return srv_fail(ABX_ERR_INVALID, "precision %d", options->precision);
   if (options->tracking < ABX_TRACK_DELTA || options->tracking > ABX_TRACK_CARTER)
     return srv_fail(ABX_ERR_INVALID, "tracking %d", options->tracking);
+  if (options->lanes < 0 || options->lanes > 16) return srv_fail(ABX_ERR_INVALID, "lanes %d out of range", options->lanes);
   abx_server* s = new abx_server();
   s->opt = *options;
   if (!s->opt.hbm_budget_bytes) s->opt.hbm_budget_bytes = 150ull * 1000 * 1000 * 1000;
-  s->worker = std::thread([s] { s->loop(); });
+  if (!s->opt.lanes) s->opt.lanes = 2;
+  if (!s->opt.history_quantum) s->opt.history_quantum = 256;
+  s->idle_lanes = s->opt.lanes;
+  for (int i = 0; i < s->opt.lanes; i++) s->lanes.emplace_back([s] { s->lane_loop(); });
   s->preparer = std::thread([s] { s->prep_loop(); });
   *out = s;
   return ABX_OK;
@@ -379,7 +430,9 @@ extern "C" int abx_server_destroy(abx_server* s) {
   s->cv_work.notify_all();
   s->cv_staged.notify_all();
   if (s->preparer.joinable()) s->preparer.join();
-  if (s->worker.joinable()) s->worker.join();
+  for (std::thread& t : s->lanes)
+    if (t.joinable()) t.join();
+  cancel_queued(s);
   if (s->staged && s->staged->prepared) abx::batch_discard(s->staged->prepared);
   delete s;
   return ABX_OK;

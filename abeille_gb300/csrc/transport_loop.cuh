@@ -203,18 +203,21 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_T
     if (TRACE) trace_rec(A, L, 7, k.cell);                                                      \
   }
 
+  uint32_t wtaken = 0;  // histories this warp took (warp-uniform)
   while (true) {
     // ---------------------------------------------------------------- refill
     const bool need = ph == PH_REFILL && !done;
     const unsigned m = __ballot_sync(0xffffffffu, need);
     if (m) {
       const unsigned leader = __ffs(m) - 1;
+      const bool quota_left = A.warp_quota == 0 || wtaken < A.warp_quota;
       unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(&st->next_hist, (unsigned long long)__popc(m));
+      if (lane == leader && quota_left) base = atomicAdd(&st->next_hist, (unsigned long long)__popc(m));
       base = __shfl_sync(0xffffffffu, base, leader);
+      wtaken += __popc(m);
       if (need) {
         const unsigned long long h = base + __popc(m & ((1u << lane) - 1u));
-        if (h >= n_hist || st->err) {
+        if (!quota_left || h >= n_hist || st->err) {
           done = true;
           ph = PH_DONE;
         } else if (!lane_load<R, SINGLE>(A, T, V, L, k, (uint32_t)h)) {

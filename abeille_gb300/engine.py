@@ -201,6 +201,11 @@ class BatchEngine(Engine):
         self.ctx = C.c_void_p()
         abi.check(self.lib.abx_create_batch(arr, len(self.builts), device, C.byref(self.ctx)), self.lib)
 
+    def set_history_quantum(self, histories_per_warp):
+        """Warps retire after this many histories so that blocks free their SM
+        slots throughout a batch run (0: persistent warps)."""
+        abi.check(self.lib.abx_set_history_quantum(self.ctx, int(histories_per_warp)), self.lib)
+
     def replace(self, builts):
         """Swap in another set of problems, keeping the device buffers."""
         builts = list(builts)
@@ -222,10 +227,10 @@ class Server:
     batched by a native scheduler thread under an HBM admission budget."""
 
     def __init__(self, device=0, precision="mixed", tracking="delta-tracking", nbatches=10, hbm_budget_bytes=0,
-                 max_round_problems=0, keep_tallies=True):
+                 max_round_problems=0, keep_tallies=True, lanes=0, history_quantum=0):
         self.lib = abi.load()
         o = abi.ServerOptions(device, abi.PRECISION[precision], abi.TRACKING[tracking], nbatches, hbm_budget_bytes,
-                              max_round_problems, int(bool(keep_tallies)))
+                              max_round_problems, int(bool(keep_tallies)), lanes, history_quantum)
         self.srv = C.c_void_p()
         abi.check(self.lib.abx_server_create(C.byref(o), C.byref(self.srv)), self.lib)
 

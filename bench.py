@@ -241,6 +241,9 @@ def main():
     ap.add_argument("--rates", default="200,1000,5000", help="config 4: Poisson arrival rates, requests/s")
     ap.add_argument("--duration", type=float, default=3.0, help="config 4: seconds of arrivals per rate")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="config 4: HBM admission budget")
+    ap.add_argument("--lanes", type=int, default=0, help="config 4: rounds on the GPU at once (0: the server's 2)")
+    ap.add_argument("--quantum", type=int, default=0,
+                    help="config 4: histories per warp before a block retires (0: the server's 256)")
     ap.add_argument("--autotune", type=int, default=-1,
                     help="configs 0-2: tune the transport launch shape on this many source histories first "
                          "(-1: one generation's histories; 0: off)")
@@ -595,7 +598,8 @@ def bench_server(args):
 
     def serve(rate, duration, record):
         srv = Server(device=local, precision=args.precision, nbatches=nb,
-                     hbm_budget_bytes=int(args.budget_gb * 1e9), keep_tallies=False)
+                     hbm_budget_bytes=int(args.budget_gb * 1e9), keep_tallies=False, lanes=args.lanes,
+                     history_quantum=args.quantum)
         done, lock = {}, threading.Lock()
         stop = threading.Event()
 
@@ -671,6 +675,7 @@ def bench_server(args):
         "dtype": "f32-track/f64-tally" if args.precision == "mixed" else "f64", "data": "synthetic",
         "config": {"workload": WORKLOADS[4], "deck": 4, "arrivals": "poisson", "rates": rates, "duration_s": args.duration,
                    "problem_pool": npool, "batches": nb, "hbm_budget_gb": args.budget_gb,
+                   "lanes": args.lanes or 2, "history_quantum": args.quantum or 256,
                    "precision": args.precision, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 at the high rates (rounds of thousands of problems)"},
         "latency": sweep,

@@ -320,6 +320,21 @@ typedef struct abx_context abx_ctx;
  * src/delta_tracker.cpp:50-70). */
 int abx_create(const abx_problem* problem, int device, abx_ctx** out);
 int abx_destroy(abx_ctx* ctx);
+
+/* The reference's multigroup YAML deck (src/parser.cpp:77-1054), read and
+ * flattened natively: abx_deck_read parses `yaml_text` (the text of an
+ * input_files/*.yaml deck) into an abx_problem owned by the returned handle
+ * (valid until abx_deck_free), with the reference parser's conventions --
+ * RPN regions, universe order, chi rows, `fissile-only` on the source entry,
+ * top-level `sampling-xs-ratio`.  `precision` is ABX_PREC_*, which decks do
+ * not carry.  ABX_ERR_INVALID with the reason in abx_last_error_string for a
+ * deck outside the multigroup path or malformed.  abx_create_from_deck reads
+ * and creates the context in one call (what the reference-side adapter of
+ * the transporter uses: it holds the deck text, not a flattened problem). */
+typedef struct abx_deck abx_deck;
+int abx_deck_read(const char* yaml_text, int precision, abx_deck** deck, const abx_problem** problem);
+int abx_deck_free(abx_deck* deck);
+int abx_create_from_deck(const char* yaml_text, int precision, int device, abx_ctx** out);
 const char* abx_last_error_string(void);
 int abx_version(int* major, int* minor, int* patch);
 
@@ -473,13 +488,18 @@ int abx_tally_read_all(abx_ctx* ctx, double* avg, double* var, size_t capacity, 
 /* ---------------------------------------------------------- request loop */
 /* A serving loop for fixed-source problems (no reference counterpart: the
  * reference runs one deck per process).  Requests are copied at submission and
- * queued; a scheduler thread admits queued requests in arrival order while
- * their estimated device footprint fits the HBM budget, transports them
- * together as one batch context (abx_create_batch + abx_run_fixed_source_batch),
- * and hands results back through abx_server_poll.  While one round runs, new
- * arrivals queue for the next.  Every request's results equal those of its
- * problem run alone: batch b of a problem always transports the same
- * histories with the same per-history random streams. */
+ * queued; a scheduler thread admits queued requests in arrival order into a
+ * round while the estimated device footprint of everything admitted and not
+ * yet finished fits the HBM budget, and `lanes` GPU threads -- each with its
+ * own batch context, stream and device buffers -- run rounds side by side
+ * (abx_run_fixed_source_batch with a history quantum, so the blocks of a
+ * running launch retire all along and a newly admitted round's launch gets
+ * their SM slots as they free up).  A request that arrives while others are
+ * on the device is admitted as soon as a lane and its share of the budget are
+ * free; its HBM share returns when its round ends.  Results come back through
+ * abx_server_poll.  Every request's results equal those of its problem run
+ * alone: batch b of a problem always transports the same histories with the
+ * same per-history random streams. */
 typedef struct abx_server abx_server;
 
 typedef struct abx_server_options {
@@ -490,6 +510,10 @@ typedef struct abx_server_options {
   uint64_t hbm_budget_bytes;  /* admission budget per round; 0: 150 GB      */
   int32_t max_round_problems; /* 0: no limit                                */
   int32_t keep_tallies;       /* copy each request's tally bins back        */
+  int32_t lanes;              /* rounds on the GPU at once, each in its own
+                                 context and stream; 0: 2                    */
+  uint32_t history_quantum;   /* histories a warp takes before its block
+                                 retires and frees its SM slot; 0: 256       */
 } abx_server_options;
 
 typedef struct abx_request_result {
@@ -517,7 +541,7 @@ typedef struct abx_server_stats {
 } abx_server_stats;
 
 int abx_server_create(const abx_server_options* options, abx_server** out);
-/* Stops admitting, finishes the running round, cancels queued requests and
+/* Stops admitting, finishes the running rounds, cancels queued requests and
  * frees everything. */
 int abx_server_destroy(abx_server* server);
 /* Copies `problem` (fixed-source, matching the server's precision and
@@ -561,6 +585,16 @@ int abx_last_transport_ms(abx_ctx* ctx, double* ms);
  * counterpart).  On by default; 0 launches the kernels one by one.  Traced
  * runs always launch directly. */
 int abx_set_graphs(abx_ctx* ctx, int enabled);
+
+/* Batch runs (abx_run_fixed_source_batch; no reference counterpart): every
+ * warp of the transport launch retires after taking `histories_per_warp`
+ * histories and the launch gets as many blocks as that needs, so blocks
+ * finish throughout the run and their SM slots go to whatever else is
+ * queued on the GPU -- the launches of other contexts' streams in the
+ * request loop.  0 (the default): persistent warps, one wave of blocks.
+ * Not applied to problems whose histories carry secondaries.  Results do
+ * not depend on it. */
+int abx_set_history_quantum(abx_ctx* ctx, uint32_t histories_per_warp);
 
 /* Transport kernel (no reference counterpart; results do not depend on it).
  * HISTORY: one lane per history, the lanes of a warp running their event

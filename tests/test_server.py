@@ -12,7 +12,7 @@ import time
 import numpy as np
 import pytest
 
-from abeille_gb300 import Engine, Server, decks
+from abeille_gb300 import BatchEngine, Engine, Server, decks
 from abeille_gb300.abi import AbxError
 
 
@@ -94,4 +94,44 @@ def test_each_request_equals_its_problem_alone(budget, max_round):
         srv.release(rid)
         alone.close()
     assert st["completed"] == len(ids) and st["failed"] == 0
+    srv.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_request_admitted_while_another_runs(precision):
+    """Continuous batching: a long request goes on the device, then short
+    ones arrive.  Each short one is admitted at once into its own round on
+    another lane, runs while the long one is still on the device (its
+    launch takes SM slots as the long launch's blocks retire) and finishes
+    first; every result equals its problem run alone in a batch context of
+    its own (the same kernels): counts bit-exact, leakage and tally bins
+    within 1e-12 relative."""
+    nb = 4
+    big = _problem(0, precision, hmax=400000 if precision == "mixed" else 100000, nb=nb)
+    small = [_problem(i, precision, hmax=800, nb=nb) for i in range(1, 4)]
+    builts = [b.build(precision=precision) for b in [big] + small]
+    srv = Server(precision=precision, nbatches=nb, lanes=3)
+    ids = [srv.submit(builts[0], tag=0)]
+    time.sleep(0.02)
+    for i, bt in enumerate(builts[1:], 1):
+        ids.append(srv.submit(bt, tag=i))
+        time.sleep(0.001)
+    got = _collect(srv, len(ids))
+    rb = got[ids[0]]
+    assert rb["status"] == 0
+    for rid in ids[1:]:
+        r = got[rid]
+        assert r["status"] == 0 and r["round"] != rb["round"], (r, rb)
+        assert r["latency_ms"] < rb["latency_ms"], (r["latency_ms"], rb["latency_ms"])
+    for i, rid in enumerate(ids):
+        r = got[rid]
+        alone = BatchEngine([builts[i]], 0)
+        (sa,), _ = alone.run(nb)
+        assert r["collisions"] == sa["collisions"] and r["flights"] == sa["flights"], i
+        assert r["histories"] == sa["histories"] == nb * ([big] + small)[i].nparticles
+        assert abs(r["leak_avg"] - sa["leak_avg"]) <= 1e-12 * abs(sa["leak_avg"]), i
+        avg, _ = srv.tally(rid, r["n_tally_bins"])
+        assert np.allclose(avg, alone.tally_all()[0], rtol=1e-12, atol=0), i
+        alone.close()
     srv.close()
