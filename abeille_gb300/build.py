@@ -1,6 +1,6 @@
 """In-tree build of the CUDA engine (sm_103a) into abeille_gb300/_lib/.
 
-Ten translation units are compiled in parallel with nvcc and linked into one
+Eleven translation units are compiled in parallel with nvcc and linked into one
 shared library exposing the C-ABI of include/abeille_gb300.h:
 
   engine.cu                   host side + bookkeeping kernels     --fmad=false
@@ -12,6 +12,7 @@ shared library exposing the C-ABI of include/abeille_gb300.h:
   transport_pool_mixed.cu     pooled (event-sorted) FP32-tracking kernels
   transport_pool_fp64.cu      pooled FP64 parity kernels               --fmad=false
   problem_tables.cpp          host table derivation (problems appended to the pools)
+  deck.cpp                    reference-format YAML decks read and flattened natively
   server.cpp                  request loop (host scheduler thread)
 
 Host code is compiled with -ffp-contract=off so derived tables round the same
@@ -42,6 +43,7 @@ UNITS = [
     ("transport_pool_mixed.cu", []),
     ("transport_pool_fp64.cu", ["--fmad=false"]),
     ("problem_tables.cpp", []),
+    ("deck.cpp", []),
     ("server.cpp", []),
 ]
 
