@@ -4,7 +4,10 @@ reference tree, against the stand-in headers of oracle/refshim/include
 (yaml-cpp, PapillonNDL, HighFive, NDArray, Boost.unordered, pcg-cpp from
 pyarrow's vendored copy) and oracle/refshim/stubs.cpp (the continuous-energy,
 plotting, cancellation and output code the multigroup path never runs),
-driven by oracle/refshim/harness.cpp.  Test infrastructure: it checks the
+driven by oracle/refshim/harness.cpp (decks arrive as JSON, oracle/refshim/
+yaml_json.cpp).  build_adapter_check() also links the reference-side
+transporter binding (include/abeille_gb300_transporter.hpp) against the same
+objects and the engine library: oracle/_ref/adapter_check.  Test infrastructure: it checks the
 oracle; nothing of the product links it.
 
 Usage: python oracle/refshim/build_ref.py [REFERENCE_ROOT]
@@ -68,7 +71,7 @@ def build(ref=None, force=False, quiet=False):
         return None
     srcs = sorted(f for f in glob.glob(os.path.join(ref, "src", "*.cpp"))
                   if os.path.splitext(os.path.basename(f))[0] not in SKIP)
-    own = [os.path.join(HERE, "harness.cpp"), os.path.join(HERE, "stubs.cpp")]
+    own = [os.path.join(HERE, "harness.cpp"), os.path.join(HERE, "stubs.cpp"), os.path.join(HERE, "yaml_json.cpp")]
     inc = ["-I", os.path.join(ref, "include"), "-I", os.path.join(HERE, "include"),
            f"-DPCG_VENDORED_HEADER=\"{pcg}\""]
     h = hashlib.sha256()
@@ -106,3 +109,37 @@ def build(ref=None, force=False, quiet=False):
 
 if __name__ == "__main__":
     print(build(sys.argv[1] if len(sys.argv) > 1 else None, force="--force" in sys.argv))
+
+
+ADAPTER = os.path.join(OUT, "adapter_check")
+
+
+def build_adapter_check(ref=None):
+    """Compile oracle/refshim/adapter_check.cpp -- the reference-side
+    GpuTransporter (include/abeille_gb300_transporter.hpp) in a program of
+    the reference's own objects -- and link it with libabeille_gb300.so.
+    Returns the program's path, or None where the reference build is not
+    available."""
+    if not build(ref):
+        return None
+    ref = ref or os.environ.get("ABEILLE_REFERENCE") or DEFAULT_REFERENCE
+    repo = os.path.dirname(ORACLE)
+    sys.path.insert(0, repo)
+    from abeille_gb300 import build as engine_build
+    lib = engine_build.build()
+    cxx = shutil.which("g++")
+    pcg = pcg_header()
+    objs = sorted(f for f in glob.glob(os.path.join(OUT, "obj", "*.o")) if not f.endswith("refshim_harness.o"))
+    src = os.path.join(HERE, "adapter_check.cpp")
+    obj = os.path.join(OUT, "adapter_check.o")
+    inc = ["-I", os.path.join(ref, "include"), "-I", os.path.join(HERE, "include"), "-I", os.path.join(repo, "include"),
+           f"-DPCG_VENDORED_HEADER=\"{pcg}\""]
+    r = subprocess.run([cxx] + FLAGS + inc + ["-c", src, "-o", obj], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("adapter check failed to compile:\n" + r.stderr[-4000:])
+    libdir = os.path.dirname(lib)
+    r = subprocess.run([cxx, "-o", ADAPTER, obj] + objs + ["-L", libdir, "-labeille_gb300", f"-Wl,-rpath,{libdir}",
+                                                           "-lpthread", "-lm"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("adapter check failed to link:\n" + r.stderr[-4000:])
+    return ADAPTER
