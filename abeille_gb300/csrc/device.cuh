@@ -222,34 +222,8 @@ template <class R> ABX_DEV R quad_dist(R a, R k, R c, R quad, bool on) {
   return d;
 }
 
-// a, k, c of a sphere or x/y/z-cylinder (the forms of sphere.cpp and
-// {x,y,z}cylinder.cpp) formed in FP64 from the position, direction and
-// surface coefficients as stored.  Near grazing incidence c = |r - r0|^2 - R^2
-// is a small difference of large squares: formed in FP32 its rounding
-// (~1e-7 R^2) rivals the discriminant itself, while in FP64 the root is the
-// exact one for the stored FP32 position.
-template <class R> ABX_DEV void quad_coeffs64(const SurfT<R>& s, V3<R> r, V3<R> u, double& a, double& k, double& c) {
-  double p, q, w = 0., up, uq, uw = 0., Rr;
-  if (s.type == ABX_SURF_SPHERE) {
-    p = (double)r.x - (double)s.c[0]; q = (double)r.y - (double)s.c[1]; w = (double)r.z - (double)s.c[2];
-    up = u.x; uq = u.y; uw = u.z; Rr = s.c[3];
-  } else if (s.type == ABX_SURF_ZCYLINDER) {
-    p = (double)r.y - (double)s.c[1]; q = (double)r.x - (double)s.c[0]; up = u.y; uq = u.x; Rr = s.c[2];
-  } else if (s.type == ABX_SURF_XCYLINDER) {
-    p = (double)r.y - (double)s.c[0]; q = (double)r.z - (double)s.c[1]; up = u.y; uq = u.z; Rr = s.c[2];
-  } else {
-    p = (double)r.x - (double)s.c[0]; q = (double)r.z - (double)s.c[1]; up = u.x; uq = u.z; Rr = s.c[2];
-  }
-  a = up * up + uq * uq + uw * uw;
-  k = p * up + q * uq + w * uw;
-  c = p * p + q * q + w * w - Rr * Rr;
-}
-
-// The reference's quadric distance (quad_dist) with a, k and c formed in
-// FP64: the mixed mode's grazing-incidence path.
-template <class R> ABX_DEV R grazing_fix(const SurfT<R>& s, V3<R> r, V3<R> u, bool on) {
-  double ad, kd, cd;
-  quad_coeffs64(s, r, u, ad, kd, cd);
+template <class R> ABX_DEV R grazing_fix(R a, R k, R c, bool on) {
+  double ad = a, kd = k, cd = c;
   double q = kd * kd - ad * cd;
   if (q < 0.) return Tol<R>::INF;
   if (on || fabs(cd) < (double)Tol<R>::SCQ) {
@@ -280,7 +254,7 @@ template <class R> ABX_DEV R surf_dist(const SurfT<R>& s, V3<R> r, V3<R> u, bool
       R k = x * u.x + y * u.y + z * u.z;
       R c = x * x + y * y + z * z - Rr * Rr;
       R quad = k * k - c;
-      if (sizeof(R) == 4 && quad >= R(0) && quad < R(1e-3) * k * k) return grazing_fix<R>(s, r, u, on);
+      if (sizeof(R) == 4 && quad >= R(0) && quad < R(1e-3) * k * k) return grazing_fix<R>(R(1), k, c, on);
       return quad_dist<R>(R(1), k, c, quad, on);
     }
     default: {
@@ -297,7 +271,7 @@ template <class R> ABX_DEV R surf_dist(const SurfT<R>& s, V3<R> r, V3<R> u, bool
       R k = p * up + q * uq;
       R c = p * p + q * q - Rr * Rr;
       R quad = k * k - a * c;
-      if (sizeof(R) == 4 && quad >= R(0) && quad < R(1e-3) * k * k) return grazing_fix<R>(s, r, u, on);
+      if (sizeof(R) == 4 && quad >= R(0) && quad < R(1e-3) * k * k) return grazing_fix<R>(a, k, c, on);
       return quad_dist<R>(a, k, c, quad, on);
     }
   }
@@ -820,19 +794,16 @@ ABX_DEV R exit_dist(const SurfT<R>& s, int32_t t, V3<R> r, V3<R> u, bool on_it) 
       }
     }
   }
-  // a, k and c themselves in FP64 from the stored position: near grazing
-  // incidence c is the small difference of large squares.
   double ad = a, kd = k, cd = c;
-  if (sizeof(R) == 4) quad_coeffs64(s, r, u, ad, kd, cd);
   double quad = kd * kd - ad * cd;
   if (t < 0) {  // inside: leave through the far root
-    if (cd > 0. && kd >= 0.) return R(0);
+    if (c > R(0) && k >= R(0)) return R(0);
     if (quad < 0.) return R(0);
     double d = (-kd + sqrt(quad)) / ad;
     return d > 0. ? (R)d : R(0);
   }
-  if (cd < 0.) return R(0);  // outside region but within the quadric
-  if (kd >= 0. || quad < 0.) return INF;
+  if (c < R(0)) return R(0);  // outside region but within the quadric
+  if (k >= R(0) || quad < 0.) return INF;
   double d = (-kd - sqrt(quad)) / ad;
   return d > 0. ? (R)d : R(0);
 }

@@ -333,11 +333,23 @@ def main():
     achieved = alg / (tr_ms / 1e3) / 1e9
     peak, src = peaks()
     hist = sum(r["histories"] for r in recs) / max(len(recs), 1)
-    tph = TRAFFIC_PER_HISTORY.get((args.config, args.precision, builder.tracking))
-    traffic = tph * hist if tph else None
+    cnt = COUNTERS.get((args.config, args.precision, builder.tracking, kernel_used))
+    traffic = cnt["dram_bytes_per_history"] * hist if cnt else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "peak_source": src,
             "kernel": "transport_kernel", "algorithmic_bytes_per_launch": alg / max(len(recs), 1)}
+    clocks = clk.summary()
+    if cnt:
+        # what binds this kernel: instruction issue, not HBM
+        import torch
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clocks.get("sm_mhz") or 2070.0
+        inst = cnt["warp_inst_per_collision"] * coll
+        roof["issue"] = {"warp_inst_per_launch": inst / max(len(recs), 1),
+                         "issue_frac": inst / (tr_ms / 1e3) / (sms * SCHEDULERS_PER_SM * mhz * 1e6),
+                         "lanes_per_inst": cnt["thread_inst_per_collision"] / cnt["warp_inst_per_collision"],
+                         "peak": f"{sms} SMs x {SCHEDULERS_PER_SM} schedulers x {mhz:.0f} MHz",
+                         "counters": cnt["source"] + " (per collision and per history, scaled to this run)"}
     cpu = None
     if world == 1 and not args.no_cpu:
         v, cores, c, dt = cpu_baseline(args.config, args.cpu_sample)
@@ -356,7 +368,7 @@ def main():
                               "grid": shape[1] if shape else None, "kernel": kernel_used}},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": KERNELS_PER_GEN * args.steps,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "flights_per_s": flights / (step_ms / 1e3) * world,
         "detail": {"flights": flights, "collisions": coll, "sites": sites, "transport_ms": tr_ms,
                    "wall_s": wall, "kcol_last": recs[-1]["kcol"], "lost": sum(r["lost"] for r in recs),
@@ -578,7 +590,7 @@ def bench_server(args):
     """Config 4: config-3 problems arriving as a Poisson stream at each rate of
     `--rates` for `--duration` s, served by the request loop (mixed
     precision); latency percentiles per rate, aggregate collisions/s, the
-    FP64 one-problem-per-launch rate, and the leakage z-scores of the served
+    one-problem-per-launch rates (mixed and FP64), and the leakage z-scores of the served
     results against FP64 runs of the same problems."""
     import threading
 
@@ -667,7 +679,7 @@ def bench_server(args):
     z = np.array([(uniq[t]["leak_avg"] - r64["leak_avg"]) / np.hypot(uniq[t]["leak_std"], r64["leak_std"])
                   for t, r64 in zip(tags, rows64) if np.hypot(uniq[t]["leak_std"], r64["leak_std"]) > 0])
     idx = np.linspace(0, npool - 1, min(args.per_problem_sample, npool)).astype(int)
-    per = _per_problem_launch(idx, nb, ["fp64"], local)
+    per = _per_problem_launch(idx, nb, sorted({args.precision, "fp64"}), local)
     line = {
         "metric": "collisions/s", "value": head["collisions_per_s"], "unit": "collisions/s", "n_gpus": world,
         "steps": len(rates), "warmup": 1, "ms_per_step": 1e3 * args.duration, "higher_is_better": True,
@@ -680,6 +692,9 @@ def bench_server(args):
                    "l2": "inputs larger than L2 at the high rates (rounds of thousands of problems)"},
         "latency": sweep,
         "per_problem_launch": per,
+        # the served rate at the highest arrival rate over one problem per
+        # launch, against the same precision and against FP64
+        "served_over_per_problem_launch": {p: head["collisions_per_s"] / v["value"] for p, v in per.items()},
         "zscore_vs_fp64": {"problems": int(z.size), "frac_abs_z_lt_2": float(np.mean(np.abs(z) < 2)),
                            "mean_z": float(z.mean())},
         "e2e": {"value": head["collisions_per_s"], "unit": "collisions/s", "h2d_bytes_per_step": None,
@@ -692,12 +707,30 @@ def bench_server(args):
     return 0
 
 
-# DRAM bytes (read + write) per history of a transport launch, from the ncu
-# captures in profiles/transport_kernel_config1_mixed_300k.md (157.6 MB at
-# 300,000 histories) and profiles/transport_kernel_config2_mixed_300k.md
-# (35.3 MB at 300,000); bank, site and spill traffic grow with the histories.
-TRAFFIC_PER_HISTORY = {(1, "mixed", "delta-tracking"): 157.60e6 / 3e5,
-                       (2, "mixed", "surface-tracking"): 35.30e6 / 3e5}
+# Counters of the transport kernel per unit of work, from ncu captures of the
+# same workloads at 300,000 histories per generation (one launch, the timed
+# generation of `bench.py --steps 1 --warmup 1 --particles 300000 --no-e2e
+# --no-cpu --no-fp64 --autotune 0`, metrics smsp__inst_executed.sum,
+# smsp__thread_inst_executed.sum, dram__bytes_read.sum + dram__bytes_write.sum,
+# divided by that launch's collisions and histories).  The bench line scales
+# them by its own collisions and histories, and divides the instructions by its
+# own device time and sampled SM clock for the fraction of the issue peak (one
+# warp instruction per scheduler per cycle, 4 schedulers per SM).
+COUNTERS = {
+    (1, "mixed", "delta-tracking", "history"): {
+        "warp_inst_per_collision": 4215668368 / 7371639, "thread_inst_per_collision": 23680295342 / 7371639,
+        "dram_bytes_per_history": (18623488 + 165544704) / 3e5,
+        "source": "profiles/transport_kernel_config1_mixed_300k.md"},
+    (2, "mixed", "surface-tracking", "history"): {
+        "warp_inst_per_collision": 3123853844 / 2419058, "thread_inst_per_collision": 30610976961 / 2419058,
+        "dram_bytes_per_history": (22607360 + 15952896) / 3e5,
+        "source": "profiles/transport_kernel_counters_300k.md"},
+    (1, "fp64", "delta-tracking", "history"): {
+        "warp_inst_per_collision": 6961345999 / 7371273, "thread_inst_per_collision": 44225291014 / 7371273,
+        "dram_bytes_per_history": (36775680 + 792786432) / 3e5,
+        "source": "profiles/transport_kernel_counters_300k.md"},
+}
+SCHEDULERS_PER_SM = 4
 L2_FLUSH_BYTES = 256 << 20
 
 if __name__ == "__main__":

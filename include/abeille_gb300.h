@@ -372,8 +372,8 @@ int abx_transport(abx_ctx* ctx, const abx_particle* bank, size_t n, double kcol,
  * All per-call scratch is one fixed 6 MB device array, reserved on every GPU
  * that loads the library and held until the process exits.  Every call uses
  * that same array, so calls that overlap on the GPU race.  The first call on
- * a device looks the array's address up; make that call before any stream
- * capture. */
+ * a device looks the array's address up.  Each call reads the step's status
+ * back and synchronises the context's stream before it returns. */
 int abx_transport_noalloc(abx_ctx* ctx, const abx_particle* bank_dev, size_t n,
                           double kcol, int converged, abx_site* sites_dev,
                           size_t site_capacity, size_t* n_sites,
