@@ -62,6 +62,9 @@ int transport_regs_f_surface();
 void launch_pool_f(const TransportArgs<float>& A, int tracking, bool iso, int grid, int block, cudaStream_t s);
 int occupancy_pool_f(int tracking, bool iso, int block);
 size_t pool_slot_bytes_f();
+// transport_pool_mixed_surface.cu: the FP32 surface-tracking pooled kernels
+void launch_pool_f_surface(const TransportArgs<float>& A, bool iso, int grid, int block, cudaStream_t s);
+int occupancy_pool_f_surface(bool iso, int block);
 void launch_pool_d(const TransportArgs<double>& A, int tracking, int grid, int block, cudaStream_t s);
 int occupancy_pool_d(int tracking, int block);
 size_t pool_slot_bytes_d();

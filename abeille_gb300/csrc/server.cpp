@@ -412,7 +412,7 @@ extern "C" int abx_server_create(const abx_server_options* options, abx_server**
   abx_server* s = new abx_server();
   s->opt = *options;
   if (!s->opt.hbm_budget_bytes) s->opt.hbm_budget_bytes = 150ull * 1000 * 1000 * 1000;
-  if (!s->opt.lanes) s->opt.lanes = 2;
+  if (!s->opt.lanes) s->opt.lanes = 3;
   if (!s->opt.history_quantum) s->opt.history_quantum = 256;
   s->idle_lanes = s->opt.lanes;
   for (int i = 0; i < s->opt.lanes; i++) s->lanes.emplace_back([s] { s->lane_loop(); });

@@ -240,8 +240,10 @@ def main():
                     help="config 3/4: problems timed one launch per problem")
     ap.add_argument("--rates", default="200,1000,5000", help="config 4: Poisson arrival rates, requests/s")
     ap.add_argument("--duration", type=float, default=3.0, help="config 4: seconds of arrivals per rate")
+    ap.add_argument("--warm", type=float, default=1.0,
+                    help="config 4: seconds of arrivals at each rate before the measured ones (same server)")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="config 4: HBM admission budget")
-    ap.add_argument("--lanes", type=int, default=0, help="config 4: rounds on the GPU at once (0: the server's 2)")
+    ap.add_argument("--lanes", type=int, default=0, help="config 4: rounds on the GPU at once (0: the server's 3)")
     ap.add_argument("--quantum", type=int, default=0,
                     help="config 4: histories per warp before a block retires (0: the server's 256)")
     ap.add_argument("--autotune", type=int, default=-1,
@@ -592,6 +594,7 @@ def bench_server(args):
     precision); latency percentiles per rate, aggregate collisions/s, the
     one-problem-per-launch rates (mixed and FP64), and the leakage z-scores of the served
     results against FP64 runs of the same problems."""
+    import gc
     import threading
 
     import __graft_entry__
@@ -609,6 +612,11 @@ def bench_server(args):
     rng = np.random.default_rng(11 + rank)
 
     def serve(rate, duration, record):
+        """One server at one Poisson rate: `--warm` s of arrivals first (the
+        server's lanes create their contexts and size their buffers), then
+        `duration` s measured.  Percentiles and rates cover the requests
+        submitted after the warm-up; the warm-up's own percentiles are kept
+        under "cold"."""
         srv = Server(device=local, precision=args.precision, nbatches=nb,
                      hbm_budget_bytes=int(args.budget_gb * 1e9), keep_tallies=False, lanes=args.lanes,
                      history_quantum=args.quantum)
@@ -623,38 +631,53 @@ def bench_server(args):
         n_sub = [10 ** 9]
         th = threading.Thread(target=poller, daemon=True)
         th.start()
-        st0 = srv.stats()
+        # the arrival process must not pause: a cyclic-GC pass in this
+        # thread would hold arrivals back and release them as one burst
+        gc.collect()
+        gc.disable()
         t0 = time.perf_counter()
         t_next, i, sub = t0, 0, {}
+        st_w, t_w = None, None
         while True:
             t_next += rng.exponential(1.0 / rate)
-            if t_next - t0 > duration:
+            if t_next - t0 > args.warm + duration:
                 break
             while time.perf_counter() < t_next:
                 pass
-            sub[srv.submit(builts[i % npool], tag=i % npool)] = time.perf_counter()
+            if st_w is None and t_next - t0 >= args.warm:
+                st_w, t_w = srv.stats(), time.perf_counter()
+            sub[srv.submit(builts[i % npool], tag=i % npool)] = time.perf_counter() - t0
             i += 1
+        gc.enable()
         n_sub[0] = len(sub)
         stop.set()
         th.join(timeout=600)
         st1 = srv.stats()
         srv.close()
-        lat = np.array([done[k][0]["latency_ms"] for k in sub if k in done])
-        t_end = max(v[1] for v in done.values()) if done else time.perf_counter()
-        coll = st1["collisions"] - st0["collisions"]
-        rows = [done[k][0] for k in sub if k in done]
-        out = {"rate": rate, "requests": len(sub), "completed": len(lat),
+        if st_w is None:
+            st_w, t_w = st1, time.perf_counter()
+        meas = [k for k in sub if k in done and sub[k] >= args.warm]
+        cold = np.array([done[k][0]["latency_ms"] for k in sub if k in done and sub[k] < args.warm])
+        lat = np.array([done[k][0]["latency_ms"] for k in meas])
+        t_end = max(done[k][1] for k in meas) if meas else time.perf_counter()
+        coll = st1["collisions"] - st_w["collisions"]
+        rows = [done[k][0] for k in meas]
+        out = {"rate": rate, "requests": len([k for k in sub if sub[k] >= args.warm]), "completed": len(lat),
                "failed": int(sum(1 for r in rows if r["status"] != 0)),
                "p50_ms": float(np.percentile(lat, 50)), "p95_ms": float(np.percentile(lat, 95)),
-               "p99_ms": float(np.percentile(lat, 99)), "collisions_per_s": coll / (t_end - t0),
-               "rounds": st1["rounds"] - st0["rounds"], "busy_ms": st1["busy_ms"] - st0["busy_ms"],
-               "transport_ms": st1["transport_ms"] - st0["transport_ms"], "collisions": coll,
-               "round_ms": {k: st1[k + "_ms"] - st0[k + "_ms"] for k in ("load", "run", "readback", "free")}}
+               "p99_ms": float(np.percentile(lat, 99)), "p999_ms": float(np.percentile(lat, 99.9)),
+               "max_ms": float(lat.max()), "collisions_per_s": coll / (t_end - t_w),
+               "rounds": st1["rounds"] - st_w["rounds"], "busy_ms": st1["busy_ms"] - st_w["busy_ms"],
+               "transport_ms": st1["transport_ms"] - st_w["transport_ms"], "collisions": coll,
+               "round_ms": {k: st1[k + "_ms"] - st_w[k + "_ms"] for k in ("load", "run", "readback", "free")},
+               "cold": {"warm_s": args.warm, "requests": int(cold.size),
+                        "p50_ms": float(np.percentile(cold, 50)) if cold.size else None,
+                        "p99_ms": float(np.percentile(cold, 99)) if cold.size else None}}
         if record is not None:
             record.extend(rows)
         return out
 
-    serve(rates[0], 0.3, None)  # warm-up
+    serve(rates[0], 0.3, None)  # process warm-up (CUDA context and modules)
     if dist:
         dist.barrier()
     sweep, served = [], []
@@ -686,8 +709,10 @@ def bench_server(args):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-track/f64-tally" if args.precision == "mixed" else "f64", "data": "synthetic",
         "config": {"workload": WORKLOADS[4], "deck": 4, "arrivals": "poisson", "rates": rates, "duration_s": args.duration,
+                   "warm_s": args.warm, "measured": "requests submitted after warm_s of arrivals at the same rate "
+                   "on the same server (steady state); the warm-up's own latencies under latency[].cold",
                    "problem_pool": npool, "batches": nb, "hbm_budget_gb": args.budget_gb,
-                   "lanes": args.lanes or 2, "history_quantum": args.quantum or 256,
+                   "lanes": args.lanes or 3, "history_quantum": args.quantum or 256,
                    "precision": args.precision, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 at the high rates (rounds of thousands of problems)"},
         "latency": sweep,
@@ -718,12 +743,12 @@ def bench_server(args):
 # warp instruction per scheduler per cycle, 4 schedulers per SM).
 COUNTERS = {
     (1, "mixed", "delta-tracking", "history"): {
-        "warp_inst_per_collision": 4215668368 / 7371639, "thread_inst_per_collision": 23680295342 / 7371639,
-        "dram_bytes_per_history": (18623488 + 165544704) / 3e5,
+        "warp_inst_per_collision": 3941494753 / 7371550, "thread_inst_per_collision": 21460652378 / 7371550,
+        "dram_bytes_per_history": (18126080 + 90729216) / 3e5,
         "source": "profiles/transport_kernel_config1_mixed_300k.md"},
     (2, "mixed", "surface-tracking", "history"): {
-        "warp_inst_per_collision": 3123853844 / 2419058, "thread_inst_per_collision": 30610976961 / 2419058,
-        "dram_bytes_per_history": (22607360 + 15952896) / 3e5,
+        "warp_inst_per_collision": 2829894961 / 2417451, "thread_inst_per_collision": 28232959555 / 2417451,
+        "dram_bytes_per_history": (22580224 + 15477760) / 3e5,
         "source": "profiles/transport_kernel_counters_300k.md"},
     (1, "fp64", "delta-tracking", "history"): {
         "warp_inst_per_collision": 6961345999 / 7371273, "thread_inst_per_collision": 44225291014 / 7371273,

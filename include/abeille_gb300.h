@@ -511,7 +511,7 @@ typedef struct abx_server_options {
   int32_t max_round_problems; /* 0: no limit                                */
   int32_t keep_tallies;       /* copy each request's tally bins back        */
   int32_t lanes;              /* rounds on the GPU at once, each in its own
-                                 context and stream; 0: 2                    */
+                                 context and stream; 0: 3                    */
   uint32_t history_quantum;   /* histories a warp takes before its block
                                  retires and frees its SM slot; 0: 256       */
 } abx_server_options;

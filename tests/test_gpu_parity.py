@@ -347,12 +347,20 @@ def test_mixed_precision_statistics_config1():
     fraction of bins with |z| < 2 is the t-distribution's P(|t| < 2): 0.950
     per pair, 0.952 pooled -- the spec bar of 95 % sits at that
     expectation.  All bins share one fission source, so the fraction of one
-    comparison moves by about a percent around it (FP64 against FP64 as
-    well: a 4x40-replica study gave mixed/FP64 pairs 0.941-0.965, mean
-    0.954, FP64/FP64 pairs 0.947-0.968).  The test therefore asserts the
-    pooled fraction and the mean over pairs against the expectation less one
-    percent, and the same FP64/FP64 control; the 95 % bar itself is read from
-    `bench.py --zscore`, which compares many more replicas."""
+    comparison scatters around it by about 0.8 % (one standard deviation)
+    even between two sets of the same precision: measured over 18 FP64/FP64
+    and mixed/mixed pairs of 40-replica sets in two studies, 0.940-0.968.
+    Every build re-draws the mixed trajectories (any change of FP32 rounding
+    sends the histories elsewhere), so a bar one percent under the
+    expectation would fail about one correct build in ten; it did once, on a
+    build whose own 9-pair study then gave a 0.9544 mean, the same as the
+    build before it.  The test therefore asserts each figure at three standard
+    deviations of that measured spread: the pooled fraction and the mean
+    over pairs within 2.5 % and 2 % of the expectation, the mean over pairs
+    within 3 % of an FP64/FP64 control drawn in the same test, and the mean z
+    (a bias would move it; every comparison measured stays within 0.025)
+    within 0.06.  The 95 % bar itself is read from `bench.py --zscore`,
+    which compares many more replicas."""
     R, n = 32, 50000
     mk = lambda: decks.config1(nparticles=n)  # noqa: E731
     sets = {}
@@ -372,10 +380,10 @@ def test_mixed_precision_statistics_config1():
           f"fp64/fp64 control {frac_c:.4f}")
     assert abs(dk) < 2, dk
     assert all(abs(p[0]) < 2 for p in pairs), pairs
-    assert frac >= _t_frac(4 * R - 2) - 0.01, frac
-    assert mean_pairs >= _t_frac(2 * R - 2) - 0.01, mean_pairs
-    assert mean_pairs >= frac_c - 0.02, (mean_pairs, frac_c)
-    assert abs(mz) < 0.1, mz
+    assert frac >= _t_frac(4 * R - 2) - 0.025, frac
+    assert mean_pairs >= _t_frac(2 * R - 2) - 0.02, mean_pairs
+    assert mean_pairs >= frac_c - 0.03, (mean_pairs, frac_c)
+    assert abs(mz) < 0.06, mz
 
 
 @pytest.mark.parametrize("tracking", ["surface-tracking", "delta-tracking"])
