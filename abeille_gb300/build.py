@@ -5,7 +5,7 @@ shared library exposing the C-ABI of include/abeille_gb300.h:
 
   engine.cu                   host side + bookkeeping kernels     --fmad=false
   transport_fp64.cu           FP64 parity transport kernels        --fmad=false
-  transport_mixed.cu          FP32-tracking kernels, delta tracking       fast div/sqrt
+  transport_mixed.cu          FP32-tracking kernels, delta tracking       fast div/sqrt, ftz
   transport_mixed_surface.cu  FP32-tracking kernels, surface tracking     fast math
   transport_mixed_variants.cu FP32-tracking kernels, implicit-leakage and Carter tracking   fast div/sqrt
   transport_mixed_branchless.cu FP32-tracking kernels, branchless collisions   fast div/sqrt
@@ -35,11 +35,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                  "-I", os.path.join(REPO, "include")]
 # FP32 tracking trades IEEE rounding of single-precision division and square
-# root for speed (measured: config 1 +23 %, config 2 +24 %), and surface
+# root for speed (measured: config 1 +23 %, config 2 +24 %; FP32 denormals
+# flushed, +1 % more on config 1 with identical results), and surface
 # tracking also takes the fast single-precision log/exp (+30 % on config 2;
 # on delta tracking it measured slower than division alone).  FP64 arithmetic
 # is unaffected by these flags.
-FAST_DIV = ["-prec-div=false", "-prec-sqrt=false"]
+FAST_DIV = ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
 FAST_MATH = ["--use_fast_math"]
 UNITS = [
     ("engine.cu", ["--fmad=false"]),

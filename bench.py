@@ -743,8 +743,8 @@ def bench_server(args):
 # warp instruction per scheduler per cycle, 4 schedulers per SM).
 COUNTERS = {
     (1, "mixed", "delta-tracking", "history"): {
-        "warp_inst_per_collision": 3941494753 / 7371550, "thread_inst_per_collision": 21460652378 / 7371550,
-        "dram_bytes_per_history": (18126080 + 90729216) / 3e5,
+        "warp_inst_per_collision": 3964713340 / 7371550, "thread_inst_per_collision": 21604900552 / 7371550,
+        "dram_bytes_per_history": (18061824 + 104158208) / 3e5,
         "source": "profiles/transport_kernel_config1_mixed_300k.md"},
     (2, "mixed", "surface-tracking", "history"): {
         "warp_inst_per_collision": 2829894961 / 2417451, "thread_inst_per_collision": 28232959555 / 2417451,
