@@ -1,10 +1,11 @@
 """In-tree build of the CUDA engine (sm_103a) into abeille_gb300/_lib/.
 
-Twelve translation units are compiled in parallel with nvcc and linked into one
+Thirteen translation units are compiled in parallel with nvcc and linked into one
 shared library exposing the C-ABI of include/abeille_gb300.h:
 
   engine.cu                   host side + bookkeeping kernels     --fmad=false
   transport_fp64.cu           FP64 parity transport kernels        --fmad=false
+  transport_fp64_wide.cu      the same, four blocks per SM (large launches)  --fmad=false
   transport_mixed.cu          FP32-tracking kernels, delta tracking       fast div/sqrt, ftz
   transport_mixed_surface.cu  FP32-tracking kernels, surface tracking     fast math
   transport_mixed_variants.cu FP32-tracking kernels, implicit-leakage and Carter tracking   fast div/sqrt
@@ -45,6 +46,7 @@ FAST_MATH = ["--use_fast_math"]
 UNITS = [
     ("engine.cu", ["--fmad=false"]),
     ("transport_fp64.cu", ["--fmad=false"]),
+    ("transport_fp64_wide.cu", ["--fmad=false"]),
     ("transport_mixed.cu", FAST_DIV),
     ("transport_mixed_surface.cu", FAST_MATH),
     ("transport_mixed_variants.cu", FAST_DIV),

@@ -262,6 +262,7 @@ struct abx_context {
   DevPools D;
   ProbT prob0{};
   bool fissile_any = false;
+  bool fp64_wide = false;  // FP64 delta/surface launches at four blocks per SM
   double* tally_gen = nullptr;
   double* tally_avg = nullptr;
   double* tally_var = nullptr;
@@ -412,6 +413,9 @@ __global__ void k_step_begin(DevState* st, unsigned long long n, double kcol, in
 
 // Exclusive scan of hist_count[0..n) (n read on the device): three phases.
 constexpr int SCAN_T = 256, SCAN_V = 8, SCAN_CHUNK = SCAN_T * SCAN_V;
+// histories per generation from which FP64 contexts use the four-block kernels:
+// about twice the 155,648 threads four 256-thread blocks on 152 SMs hold
+constexpr double FP64_WIDE_MIN_HISTORIES = 300000.;
 __global__ void k_scan_reduce(const uint32_t* in, const DevState* st, uint32_t* bsum) {
   __shared__ uint32_t sh[SCAN_T];
   const unsigned long long n = st->n_hist;
@@ -861,10 +865,11 @@ static int check_state(abx_ctx* c) {
 }
 
 // which transport kernel: the tracking mode, plus the branchless-collision
-// bit, plus the single-problem bit outside runs that score per problem
+// bit, plus the single-problem bit outside runs that score per problem, plus
+// the four-block bit of large FP64 contexts
 static int kernel_code(const abx_ctx* c) {
   return c->prob0.tracking | (c->prob0.branchless ? ABX_KERNEL_BRANCHLESS : 0) |
-         (c->batch_scores ? 0 : ABX_KERNEL_SINGLE);
+         (c->batch_scores ? 0 : ABX_KERNEL_SINGLE) | (c->fp64_wide ? ABX_KERNEL_WIDE : 0);
 }
 
 template <class R> static TransportArgs<R> make_args(abx_ctx* c, const BankT<R>& bank, const SiteT<R>& sites,
@@ -957,6 +962,11 @@ static int create_ctx(const abx_problem* problems, int nprob, int device, abx_ct
     return fail(ABX_ERR_INVALID, "precision %d", prec);
   }
   c->prec = prec;
+  // generations large enough to fill four FP64 blocks per SM twice over run
+  // the four-block FP64 kernels (transport_fp64_wide.cu)
+  c->fp64_wide = prec == ABX_PREC_FP64 && !c->prob0.branchless &&
+                 (c->prob0.tracking == ABX_TRACK_DELTA || c->prob0.tracking == ABX_TRACK_SURFACE) &&
+                 problem->settings.nparticles >= FP64_WIDE_MIN_HISTORIES;
   auto bail = [&](int code) {
     ctx_free(c);
     return code;

@@ -64,7 +64,8 @@ enum : int { ABX_PSCORES = 5, ABX_PCOUNTS = 4 };
 // bits: branchless collisions; one problem without per-problem scores (every
 // history of the launch belongs to problem 0, the batch bookkeeping compiled
 // out)
-enum : int { ABX_KERNEL_BRANCHLESS = 0x100, ABX_KERNEL_SINGLE = 0x200 };  // counters: collisions flights histories lost
+// ABX_KERNEL_WIDE: the FP64 instantiation with four blocks per SM, for large launches
+enum : int { ABX_KERNEL_BRANCHLESS = 0x100, ABX_KERNEL_SINGLE = 0x200, ABX_KERNEL_WIDE = 0x800 };  // counters: collisions flights histories lost
 
 template <class R> ABX_DEV View<R> make_view(const Tables& T);
 template <> ABX_DEV View<double> make_view<double>(const Tables& T) {

@@ -39,6 +39,9 @@ void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace
 void launch_sources(const SourceArgs& A, cudaStream_t s);
 void launch_sources_f(const SourceArgs& A, cudaStream_t s);  // transport_mixed.cu
 int transport_regs_d(int tracking);
+// transport_fp64_wide.cu: the FP64 delta/surface kernels at four blocks per SM
+void launch_transport_d_wide(const TransportArgs<double>& A, int tracking, int grid, int block, cudaStream_t s);
+int occupancy_d_wide(int tracking, int block);
 
 // transport_mixed.cu (+ transport_mixed_surface.cu); `iso`: every material
 // of the problem scatters isotropically; `tracking` is a kernel code (the

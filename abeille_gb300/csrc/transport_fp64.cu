@@ -21,7 +21,9 @@ template __global__ void transport_kernel<double, ABX_TRACK_SURFACE | ABX_KERNEL
 void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace, int grid, int block,
                         cudaStream_t s) {
   tracking &= ~ABX_KERNEL_SINGLE;  // FP64 kernels serve single problems and batches alike
-  if (tracking == (ABX_TRACK_DELTA | ABX_KERNEL_BRANCHLESS)) {
+  if (tracking & ABX_KERNEL_WIDE) {
+    launch_transport_d_wide(A, tracking, grid, block, s);
+  } else if (tracking == (ABX_TRACK_DELTA | ABX_KERNEL_BRANCHLESS)) {
     transport_kernel<double, ABX_TRACK_DELTA | ABX_KERNEL_BRANCHLESS, false><<<grid, block, 0, s>>>(A);
   } else if (tracking == (ABX_TRACK_SURFACE | ABX_KERNEL_BRANCHLESS)) {
     transport_kernel<double, ABX_TRACK_SURFACE | ABX_KERNEL_BRANCHLESS, false><<<grid, block, 0, s>>>(A);
@@ -39,6 +41,7 @@ void launch_transport_d(const TransportArgs<double>& A, int tracking, bool trace
 int occupancy_d(int tracking, int block) {
   int nb = 0;
   tracking &= ~ABX_KERNEL_SINGLE;
+  if (tracking & ABX_KERNEL_WIDE) return occupancy_d_wide(tracking, block);
   if (tracking == (ABX_TRACK_DELTA | ABX_KERNEL_BRANCHLESS))
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &nb, transport_kernel<double, ABX_TRACK_DELTA | ABX_KERNEL_BRANCHLESS, false>, block, 0);

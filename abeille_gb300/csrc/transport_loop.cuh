@@ -144,11 +144,13 @@ ABX_DEV void history_end(const TransportArgs<R>& A, const Lane<R>& L, Acc<R>& ac
 // Occupancy (measured on the 51x51-pin assembly and the 70-group
 // nested-cylinder lattice): FP32 delta tracking (and implicit-leakage delta
 // tracking) runs four 256-thread blocks per SM (64 registers), FP32 surface
-// tracking three (80 registers), FP64 three (80).
+// tracking three (80 registers), FP64 three (80) or, for large launches
+// (ABX_KERNEL_WIDE), four (64).
 // TRACK: the tracking mode, or'd with ABX_KERNEL_BRANCHLESS for the
 // branchless collisions of the branchless k-eigenvalue simulation.
 template <class R, int TRACK, bool ISO>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_TRACK_SURFACE ? 4 : 3) : 3)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? ((TRACK & 0xff) != ABX_TRACK_SURFACE ? 4 : 3)
+                                                    : ((TRACK & ABX_KERNEL_WIDE) ? 4 : 3))
     transport_kernel(const __grid_constant__ TransportArgs<R> A) {
   constexpr int TRK = TRACK & 0xff;
   constexpr bool BL = (TRACK & ABX_KERNEL_BRANCHLESS) != 0;
