@@ -751,8 +751,8 @@ COUNTERS = {
         "dram_bytes_per_history": (22580224 + 15477760) / 3e5,
         "source": "profiles/transport_kernel_counters_300k.md"},
     (1, "fp64", "delta-tracking", "history"): {
-        "warp_inst_per_collision": 6961345999 / 7371273, "thread_inst_per_collision": 44225291014 / 7371273,
-        "dram_bytes_per_history": (36775680 + 792786432) / 3e5,
+        "warp_inst_per_collision": 7450495716 / 7371273, "thread_inst_per_collision": 44965331919 / 7371273,
+        "dram_bytes_per_history": (361392384 + 3245730304) / 3e5,
         "source": "profiles/transport_kernel_counters_300k.md"},
 }
 SCHEDULERS_PER_SM = 4
