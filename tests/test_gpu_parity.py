@@ -345,7 +345,7 @@ def test_mixed_precision_statistics_config1():
     of freedom per pair) and one pooled comparison (64 against 64 replicas,
     126 degrees of freedom).  For two samples of one distribution the
     fraction of bins with |z| < 2 is the t-distribution's P(|t| < 2): 0.950
-    per pair, 0.952 pooled -- the spec bar of 95 % sits at that
+    per pair, 0.952 pooled -- the acceptance bar of 95 % sits at that
     expectation.  All bins share one fission source, so the fraction of one
     comparison scatters around it by about 0.8 % (one standard deviation)
     even between two sets of the same precision: measured over 18 FP64/FP64
