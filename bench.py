@@ -638,17 +638,19 @@ def bench_server(args):
         t0 = time.perf_counter()
         t_next, i, sub = t0, 0, {}
         st_w, t_w = None, None
-        while True:
-            t_next += rng.exponential(1.0 / rate)
-            if t_next - t0 > args.warm + duration:
-                break
-            while time.perf_counter() < t_next:
-                pass
-            if st_w is None and t_next - t0 >= args.warm:
-                st_w, t_w = srv.stats(), time.perf_counter()
-            sub[srv.submit(builts[i % npool], tag=i % npool)] = time.perf_counter() - t0
-            i += 1
-        gc.enable()
+        try:
+            while True:
+                t_next += rng.exponential(1.0 / rate)
+                if t_next - t0 > args.warm + duration:
+                    break
+                while time.perf_counter() < t_next:
+                    pass
+                if st_w is None and t_next - t0 >= args.warm:
+                    st_w, t_w = srv.stats(), time.perf_counter()
+                sub[srv.submit(builts[i % npool], tag=i % npool)] = time.perf_counter() - t0
+                i += 1
+        finally:
+            gc.enable()
         n_sub[0] = len(sub)
         stop.set()
         th.join(timeout=600)
