@@ -65,3 +65,19 @@ def test_create_without_gpu_fails_cleanly():
         pytest.skip("a GPU is present")
     assert rc == 6 and not ctx.value
     assert b"CUDA" in lib.abx_last_error_string()
+
+
+def test_fp64_units_keep_ieee_arithmetic():
+    """The FP64 parity kernels reproduce the reference per history only if no
+    multiply-add is contracted and no approximate division or square root is
+    used: every unit that compiles FP64 transport code takes --fmad=false and
+    none of the fast FP32 flags; the fast flags go to FP32-tracking units only."""
+    from abeille_gb300 import build
+    fast = set(build.FAST_DIV) | set(build.FAST_MATH)
+    units = dict(build.UNITS)
+    for u in ("engine.cu", "transport_fp64.cu", "transport_fp64_wide.cu", "transport_pool_fp64.cu"):
+        assert "--fmad=false" in units[u], u
+        assert not fast & set(units[u]), u
+    for u, flags in units.items():
+        if fast & set(flags):
+            assert u.startswith("transport_mixed") or u.startswith("transport_pool_mixed"), u
