@@ -250,7 +250,7 @@ def main():
                     help="configs 0-2: tune the transport launch shape on this many source histories first "
                          "(-1: one generation's histories; 0: off)")
     ap.add_argument("--zscore", type=int, default=0,
-                    help="config 1: compare mixed and FP64 over sets of this many replicas instead of timing")
+                    help="configs 0-2: compare mixed and FP64 over sets of this many replicas instead of timing")
     ap.add_argument("--zsets", type=int, default=1, help="with --zscore: replica sets per precision")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -528,7 +528,8 @@ def _per_problem_launch(idx, nb, precisions, device, tracking=None):
 
 
 def bench_zscore(args):
-    """Mixed against FP64 on config 1 over independent replicas: `--zsets` S
+    """Mixed against FP64 on `--config` (1 unless given; `--tracking` applies)
+    over independent replicas: `--zsets` S
     sets of `--zscore` R replicas per precision (own seed each; `--particles`
     histories per generation, default 1e5, 10 inactive + 40 active
     generations).  Every pair of sets is compared: k difference in sigma and
@@ -554,7 +555,9 @@ def bench_zscore(args):
         for prec in ("fp64", "mixed"):
             ks, avgs = [], []
             for rep in range(R):
-                b = decks.config1(nparticles=npart)
+                b = decks.CONFIGS[args.config](nparticles=npart)
+                if args.tracking:
+                    b.tracking = args.tracking
                 b.seed = 20000 + 100000 * si + (50000 if prec == "mixed" else 0) + rep
                 eng = Engine(b.build(precision=prec), 0)
                 st, _, _ = eng.run_power_iteration(50, 10)
@@ -578,7 +581,8 @@ def bench_zscore(args):
         f = [p["frac_abs_z_lt_2"] for p in pairs if p["kind"] == kind]
         if f:
             summ[kind] = {"pairs": len(f), "frac_min": min(f), "frac_max": max(f), "frac_mean": round(float(np.mean(f)), 4)}
-    line = {"metric": "mixed vs fp64 agreement", "workload": WORKLOADS[1], "replicas_per_set": R, "sets_per_precision": S,
+    line = {"metric": "mixed vs fp64 agreement", "workload": WORKLOADS[args.config], "deck": args.config,
+            "tracking": b.tracking, "replicas_per_set": R, "sets_per_precision": S,
             "histories_per_generation": npart, "generations": "10 inactive + 40 active",
             "k_mixed": float(np.mean([sets[k][0].mean() for k in sets if k.startswith("mixed")])),
             "k_fp64": float(np.mean([sets[k][0].mean() for k in sets if k.startswith("fp64")])),
