@@ -304,7 +304,7 @@ def main():
         # the bank of the generation after the timed ones (the converged
         # source, the same workload as the timed generations)
         bank, kcol = eng.read_source_bank()
-        v, h2d, d2h = e2e_measure(eng, bank, kcol, max(2, args.steps // 3), 1)
+        v, h2d, d2h = e2e_measure(eng, bank, kcol, max(5, args.steps // 2), 2)
         e2e = {"value": v * world, "unit": "collisions/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     fp64 = None
