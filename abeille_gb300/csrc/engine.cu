@@ -775,6 +775,30 @@ static int ensure_sites(abx_ctx* c, size_t n, bool mixed) {
   return ABX_OK;
 }
 
+// The AoS staging buffers of the C-ABI's host records grow with headroom,
+// like the work buffers: a reallocation's cudaFree waits for the whole device,
+// and bank sizes move from one call to the next.
+static int ensure_aos_in(abx_ctx* c, size_t n) {
+  if (c->aos_in_cap >= n) return ABX_OK;
+  if (c->aos_in) cudaFree(c->aos_in);
+  c->aos_in = nullptr;
+  c->aos_in_cap = 0;
+  const size_t cap = headroom(n);
+  CUDA_TRY(cudaMalloc(&c->aos_in, cap * sizeof(abx_particle)));
+  c->aos_in_cap = cap;
+  return ABX_OK;
+}
+static int ensure_aos_out(abx_ctx* c, size_t n) {
+  if (c->aos_out_cap >= n) return ABX_OK;
+  if (c->aos_out) cudaFree(c->aos_out);
+  c->aos_out = nullptr;
+  c->aos_out_cap = 0;
+  const size_t cap = headroom(n);
+  CUDA_TRY(cudaMalloc(&c->aos_out, cap * sizeof(abx_site)));
+  c->aos_out_cap = cap;
+  return ABX_OK;
+}
+
 static int kernel_code(const abx_ctx* c);
 
 // Histories of this context can put particles on a secondary stack:
@@ -1066,12 +1090,7 @@ extern "C" int abx_sample_sources(abx_ctx* c, uint64_t first, size_t n, abx_part
   S.x = b.x; S.y = b.y; S.z = b.z; S.ux = b.ux; S.uy = b.uy; S.uz = b.uz; S.E = b.E; S.w = b.w; S.w2 = b.w2;
   S.rng = b.rng; S.hid = b.hid; S.fam = b.fam; S.probv = nullptr; S.out_off = 0; S.st = c->st;
   launch_sources(S, c->stream);
-  if (c->aos_in_cap < n) {
-    if (c->aos_in) cudaFree(c->aos_in);
-    c->aos_in = nullptr;
-    CUDA_TRY(cudaMalloc(&c->aos_in, n * sizeof(abx_particle)));
-    c->aos_in_cap = n;
-  }
+  if ((rc = ensure_aos_in(c, n)) != ABX_OK) return rc;
   k_bank_to_aos<double><<<grid_for(n), 256, 0, c->stream>>>(b, n, c->aos_in);
   CUDA_TRY(cudaGetLastError());
   if ((rc = check_state(c)) != ABX_OK) return rc;
@@ -1096,12 +1115,7 @@ extern "C" int abx_transport(abx_ctx* c, const abx_particle* bank, size_t n, dou
   size_t scap = keig ? std::max<size_t>(site_capacity, 1) : 1;
   if ((rc = ensure_sites(c, scap, mixed)) != ABX_OK) return rc;
   if ((rc = ensure_sec(c, mixed)) != ABX_OK) return rc;
-  if (c->aos_in_cap < cap) {
-    if (c->aos_in) cudaFree(c->aos_in);
-    c->aos_in = nullptr;
-    CUDA_TRY(cudaMalloc(&c->aos_in, cap * sizeof(abx_particle)));
-    c->aos_in_cap = cap;
-  }
+  if ((rc = ensure_aos_in(c, cap)) != ABX_OK) return rc;
   if (n) CUDA_TRY(cudaMemcpyAsync(c->aos_in, bank, n * sizeof(abx_particle), cudaMemcpyHostToDevice, c->stream));
   if (mixed) k_bank_from_aos<float><<<grid_for(n), 256, 0, c->stream>>>(c->aos_in, n, c->bf[0].b);
   else k_bank_from_aos<double><<<grid_for(n), 256, 0, c->stream>>>(c->aos_in, n, c->bd[0].b);
@@ -1132,12 +1146,7 @@ extern "C" int abx_transport(abx_ctx* c, const abx_particle* bank, size_t n, dou
     return fail(ABX_ERR_CAPACITY, "fission bank capacity %zu < %zu sites", site_capacity, ns);
   if (keig && ns && sites) {
     launch_scan(c, n);
-    if (c->aos_out_cap < ns) {
-      if (c->aos_out) cudaFree(c->aos_out);
-      c->aos_out = nullptr;
-      CUDA_TRY(cudaMalloc(&c->aos_out, ns * sizeof(abx_site)));
-      c->aos_out_cap = ns;
-    }
+    if ((rc = ensure_aos_out(c, ns)) != ABX_OK) return rc;
     if (mixed) k_sites_to_aos<float><<<grid_for(ns), 256, 0, c->stream>>>(c->sf.s, c->st, c->offsets, c->bf[0].b, c->aos_out, ns);
     else k_sites_to_aos<double><<<grid_for(ns), 256, 0, c->stream>>>(c->sd.s, c->st, c->offsets, c->bd[0].b, c->aos_out, ns);
     CUDA_TRY(cudaGetLastError());
@@ -1672,12 +1681,9 @@ static int comb_generation(abx_ctx* c, bool mixed, int nxt, int g, GlobalStream&
   if ((rc = check_state(c)) != ABX_OK) return rc;
   const size_t ns = (size_t)c->st_host->n_hist;
   std::vector<abx_particle> bank(ns);
-  if (c->aos_in_cap < std::max(ns, cap)) {
-    if (c->aos_in) cudaFree(c->aos_in);
-    c->aos_in = nullptr;
-    c->aos_in_cap = 0;
-    CUDA_TRY(cudaMalloc(&c->aos_in, std::max(ns, cap) * sizeof(abx_particle)));
-    c->aos_in_cap = std::max(ns, cap);
+  {
+    const int rc_in = ensure_aos_in(c, std::max(ns, cap));
+    if (rc_in != ABX_OK) return rc_in;
   }
   if (ns) {
     if (mixed) k_bank_to_aos<float><<<grid_for(ns), 256, 0, c->stream>>>(c->bf[nxt].b, ns, c->aos_in);
@@ -1773,12 +1779,9 @@ static int load_restart_bank(abx_ctx* c, bool mixed, size_t cap, size_t* n_out) 
   }
   // the run's nparticles (set from the bank's total weight) on the device
   CUDA_TRY(cudaMemcpyAsync((void*)c->D.T.probs, &c->P.probs[0], sizeof(ProbT), cudaMemcpyHostToDevice, c->stream));
-  if (c->aos_in_cap < n) {
-    if (c->aos_in) cudaFree(c->aos_in);
-    c->aos_in = nullptr;
-    c->aos_in_cap = 0;
-    CUDA_TRY(cudaMalloc(&c->aos_in, n * sizeof(abx_particle)));
-    c->aos_in_cap = n;
+  {
+    const int rc_in = ensure_aos_in(c, n);
+    if (rc_in != ABX_OK) return rc_in;
   }
   CUDA_TRY(cudaMemcpyAsync(c->aos_in, bank.data(), n * sizeof(abx_particle), cudaMemcpyHostToDevice, c->stream));
   if (mixed) k_bank_from_aos<float><<<grid_for(n), 256, 0, c->stream>>>(c->aos_in, n, c->bf[0].b);
@@ -1955,12 +1958,9 @@ extern "C" int abx_read_source_bank(abx_ctx* c, abx_particle* out, size_t capaci
   if (!out || n == 0) return ABX_OK;
   if (capacity < n) return fail(ABX_ERR_CAPACITY, "source bank of %zu particles, capacity %zu", n, capacity);
   cudaSetDevice(c->device);
-  if (c->aos_in_cap < n) {
-    if (c->aos_in) cudaFree(c->aos_in);
-    c->aos_in = nullptr;
-    c->aos_in_cap = 0;
-    CUDA_TRY(cudaMalloc(&c->aos_in, n * sizeof(abx_particle)));
-    c->aos_in_cap = n;
+  {
+    const int rc_in = ensure_aos_in(c, n);
+    if (rc_in != ABX_OK) return rc_in;
   }
   if (mixed_of(c)) k_bank_to_aos<float><<<grid_for(n), 256, 0, c->stream>>>(c->bf[c->pi_bank].b, n, c->aos_in);
   else k_bank_to_aos<double><<<grid_for(n), 256, 0, c->stream>>>(c->bd[c->pi_bank].b, n, c->aos_in);
